@@ -1,0 +1,744 @@
+// fp_engine: the C ABI of include/firepony_gb300.h. Owns the device-resident reference, known sites and
+// covariate tables, runs the per-batch kernel sequence on one CUDA stream and finalizes the tables.
+//
+// Per batch (replacing batch->download + firepony_process_batch, device/pipeline_interface.cu:206-220 and
+// device/pipeline.cu:56-147):
+//   H2D inputs -> validate + CIGAR-length scan -> [sync: errors, event count]
+//   -> K1 prep (filters, CIGAR expansion, windows, error vectors, base/known-site masks, BAQ work lists)
+//   -> [sync: work-list sizes] -> K2 BAQ (FP32 with FP64 escalation, or plain FP64) + cap/recode
+//   -> K3 count (observations, entry counts) -> scan -> [sync: entry count]
+//   -> K3 emit -> K4 stable radix sort + ordered fold into the resident mismatch table.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "firepony_gb300.h"
+#include "kernels.h"
+
+using namespace fpg;
+
+extern "C" fp_status fp_report_write(const char *path, const fp_table_view *tables, const char *const *rg_names,
+                                     uint32_t num_rg_names, int disable_rounding, int vmaj, int vmin, int vrev);
+
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = bytes + bytes / 4 + 256;
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    template <typename T> T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+struct HostTable {
+    std::vector<uint32_t> keys;
+    std::vector<uint64_t> obs;
+    std::vector<double> mism, exp, est, emp;
+};
+
+double log10_factorial(uint64_t x) { return double(lgammaf(float(double(x + 1)))) * log10(M_E); }
+
+// log10BinomialCoefficient of the (capped) row counts (device/empirical_quality.cu:77-112, :165-174)
+double binomial_coef(uint64_t observations, double mismatches) {
+    uint64_t k = uint64_t(mismatches + 0.5) + 1;
+    uint64_t n = observations + 1 + 1;
+    const uint32_t MAXOBS = 2147483647u - 1;
+    if (n > MAXOBS) {
+        const double fraction = double(MAXOBS) / double(n);
+        k = uint64_t(round(double(k) * fraction));
+        n = MAXOBS;
+    }
+    return log10_factorial(n) - log10_factorial(k) - log10_factorial(n - k);
+}
+
+double gaussian(double value) {  // device/empirical_quality.cu:43-53
+    const double a = 0.0, b = 0.9, c = 0.0, d = 0.5;
+    return a + b * pow(double(M_E), -(pow(value - c, 2.0) / (2 * d * d)));
+}
+
+}  // namespace
+
+struct fp_engine {
+    int device = 0;
+    int baq_mode = FP_BAQ_FP32;
+    uint32_t n_rg = 1;
+    cudaStream_t st = nullptr;
+    std::string err;
+    bool finalized = false;
+
+    // resident reference and known sites
+    std::vector<DevContig> h_contigs;
+    std::vector<DevBuf> contig_bufs;
+    DevBuf d_contigs;
+    std::vector<DevSites> h_sites;
+    std::vector<DevBuf> site_bufs;
+    DevBuf d_sites;
+    DevRef ref{};
+
+    // tables
+    Tables tables{};
+    DevBuf tab_obs, tab_mism;
+
+    // batch buffers
+    DevBuf in_buf;
+    DevBatch batch{};
+    DevBuf oplen, cigoff, ev_rc, ev_type, per_read, per_base, lists, counters, entry_cnt, entry_off;
+    DevBuf entries, entries_alt, sort_tmp, scan_tmp, s32, s64;
+    u64 s64_doubles = 0;
+    BatchWork work{};
+    uint32_t last_R = 0;
+    uint64_t last_Q = 0;
+
+    // finalized tables
+    HostTable out[4];
+
+    // statistics
+    fp_stats stats{};
+    unsigned long long launch_base = 0;
+    cudaEvent_t ev[10]{};
+    HmmConst hmm{};
+    double qual2err[256];
+
+    fp_status fail(fp_status s, const std::string &m) {
+        err = m;
+        return s;
+    }
+    fp_status cuda_fail(cudaError_t e, const char *where) {
+        err = std::string(where) + ": " + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? FP_OOM : FP_DEVICE_ERROR;
+    }
+};
+
+#define CK(call, where)                                          \
+    do {                                                         \
+        cudaError_t _e = (call);                                 \
+        if (_e != cudaSuccess) return eng->cuda_fail(_e, where); \
+    } while (0)
+
+namespace {
+
+size_t al(size_t x) { return (x + 255) & ~size_t(255); }
+
+fp_status alloc_tables(fp_engine *eng) {
+    eng->tables.ks = make_keyspace(eng->n_rg);
+    const size_t n = eng->tables.ks.total;
+    CK(eng->tab_obs.ensure(n * sizeof(unsigned long long)), "table allocation");
+    CK(eng->tab_mism.ensure(n * sizeof(float)), "table allocation");
+    CK(cudaMemsetAsync(eng->tab_obs.p, 0, n * sizeof(unsigned long long), eng->st), "table clear");
+    CK(cudaMemsetAsync(eng->tab_mism.p, 0, n * sizeof(float), eng->st), "table clear");
+    eng->tables.obs = eng->tab_obs.as<unsigned long long>();
+    eng->tables.mism = eng->tab_mism.as<float>();
+    return FP_OK;
+}
+
+fp_status upload_refs(fp_engine *eng) {
+    CK(eng->d_contigs.ensure(std::max<size_t>(1, eng->h_contigs.size()) * sizeof(DevContig)), "contig table");
+    if (!eng->h_contigs.empty())
+        CK(cudaMemcpy(eng->d_contigs.p, eng->h_contigs.data(), eng->h_contigs.size() * sizeof(DevContig),
+                      cudaMemcpyHostToDevice), "contig table");
+    CK(eng->d_sites.ensure(std::max<size_t>(1, eng->h_sites.size()) * sizeof(DevSites)), "site table");
+    if (!eng->h_sites.empty())
+        CK(cudaMemcpy(eng->d_sites.p, eng->h_sites.data(), eng->h_sites.size() * sizeof(DevSites),
+                      cudaMemcpyHostToDevice), "site table");
+    eng->ref.contigs = eng->d_contigs.as<DevContig>();
+    eng->ref.num_contigs = uint32_t(eng->h_contigs.size());
+    eng->ref.sites = eng->d_sites.as<DevSites>();
+    eng->ref.num_site_contigs = uint32_t(eng->h_sites.size());
+    return FP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+fp_status fp_engine_create(const fp_options *o, fp_engine **out) {
+    if (!o || !out) return FP_BAD_INPUT;
+    *out = nullptr;
+    if (o->num_read_groups == 0 || o->num_read_groups > 256) return FP_BAD_INPUT;
+    fp_engine *eng = new fp_engine();
+    eng->device = o->device;
+    eng->baq_mode = o->baq_mode;
+    eng->n_rg = o->num_read_groups;
+    cudaError_t e = cudaSetDevice(eng->device);
+    if (e != cudaSuccess) {
+        delete eng;
+        return FP_DEVICE_ERROR;
+    }
+    e = cudaStreamCreateWithFlags(&eng->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete eng;
+        return FP_DEVICE_ERROR;
+    }
+    for (auto &x : eng->ev) cudaEventCreate(&x);
+    // host libm constants (device/baq.cu:80, :355-359; device/expected_error.h:48-51)
+    for (int q = 0; q < 256; q++) {
+        eng->hmm.qual2prob[q] = pow(10.0, -q / 10.0);
+        eng->qual2err[q] = pow(10.0, q / -10.0);
+    }
+    eng->hmm.gap_open = pow(10.0, (-40.0) / 10.);
+    baq64_set_constants(eng->hmm);
+    baq32_set_constants(eng->hmm);
+    EmpConst ec;
+    for (int d = 0; d <= 40; d++) ec.prior[d] = log10(gaussian(double(d)));
+    for (int bin = 0; bin <= 60; bin++) {
+        const double Qemp = bin / 1.0;
+        ec.log10p[bin] = Qemp / -10.0;
+        ec.log10_one_minus_p[bin] = log10(1 - pow(10.0, ec.log10p[bin]));
+    }
+    post_set_constants(ec, eng->qual2err);
+    eng->launch_base = g_kernel_launches;
+    fp_status s = alloc_tables(eng);
+    if (s == FP_OK) s = upload_refs(eng);
+    if (s == FP_OK) {
+        e = cudaStreamSynchronize(eng->st);
+        if (e != cudaSuccess) s = FP_DEVICE_ERROR;
+    }
+    if (s != FP_OK) {
+        fp_engine_destroy(eng);
+        return s;
+    }
+    *out = eng;
+    return FP_OK;
+}
+
+void fp_engine_destroy(fp_engine *eng) {
+    if (!eng) return;
+    cudaSetDevice(eng->device);
+    if (eng->st) cudaStreamSynchronize(eng->st);
+    for (auto &b : eng->contig_bufs) b.release();
+    for (auto &b : eng->site_bufs) b.release();
+    DevBuf *bufs[] = {&eng->d_contigs, &eng->d_sites, &eng->tab_obs, &eng->tab_mism, &eng->in_buf, &eng->oplen,
+                      &eng->cigoff, &eng->ev_rc, &eng->ev_type, &eng->per_read, &eng->per_base, &eng->lists,
+                      &eng->counters, &eng->entry_cnt, &eng->entry_off, &eng->entries, &eng->entries_alt,
+                      &eng->sort_tmp, &eng->scan_tmp, &eng->s32, &eng->s64};
+    for (DevBuf *b : bufs) b->release();
+    for (auto &x : eng->ev)
+        if (x) cudaEventDestroy(x);
+    if (eng->st) cudaStreamDestroy(eng->st);
+    delete eng;
+}
+
+const char *fp_last_error(const fp_engine *eng) { return eng ? eng->err.c_str() : "null engine"; }
+
+fp_status fp_engine_set_contig(fp_engine *eng, uint32_t id, const uint32_t *packed4, uint64_t n) {
+    if (!eng || (!packed4 && n)) return FP_BAD_INPUT;
+    CK(cudaSetDevice(eng->device), "set device");
+    if (id >= eng->h_contigs.size()) {
+        eng->h_contigs.resize(id + 1, DevContig{nullptr, 0});
+        eng->contig_bufs.resize(id + 1);
+    }
+    const size_t words = (n + 7) / 8;
+    DevBuf &b = eng->contig_bufs[id];
+    b.release();
+    CK(b.ensure((words + 1) * sizeof(uint32_t)), "contig upload");
+    CK(cudaMemset(b.p, 0, (words + 1) * sizeof(uint32_t)), "contig upload");
+    if (words) {
+        CK(cudaMemcpy(b.p, packed4, words * sizeof(uint32_t), cudaMemcpyHostToDevice), "contig upload");
+        if (n % 8) {
+            // symbols past the end of the contig read as 0
+            uint32_t last = packed4[words - 1] & ((1u << ((n % 8) * 4)) - 1);
+            CK(cudaMemcpy(b.as<uint32_t>() + words - 1, &last, 4, cudaMemcpyHostToDevice), "contig upload");
+        }
+    }
+    eng->h_contigs[id] = DevContig{b.as<uint32_t>(), n};
+    return upload_refs(eng);
+}
+
+fp_status fp_engine_set_known_sites(fp_engine *eng, uint32_t id, const uint32_t *start, const uint32_t *stop,
+                                    uint32_t n) {
+    if (!eng || ((!start || !stop) && n)) return FP_BAD_INPUT;
+    CK(cudaSetDevice(eng->device), "set device");
+    if (id >= eng->h_sites.size()) {
+        eng->h_sites.resize(id + 1, DevSites{nullptr, nullptr, nullptr, 0, 0});
+        eng->site_bufs.resize(id + 1);
+    }
+    // prefix max of the stops (loader/variants.cu:126-134); sites must be sorted by start
+    std::vector<uint32_t> maxend(n);
+    for (uint32_t i = 0; i < n; i++) {
+        if (i && start[i] < start[i - 1]) return eng->fail(FP_BAD_INPUT, "known sites must be sorted by start");
+        maxend[i] = i ? std::max(maxend[i - 1], stop[i]) : stop[0];
+    }
+    DevBuf &b = eng->site_bufs[id];
+    b.release();
+    CK(b.ensure(std::max<size_t>(1, size_t(n)) * 3 * sizeof(uint32_t)), "known-site upload");
+    uint32_t *p = b.as<uint32_t>();
+    if (n) {
+        CK(cudaMemcpy(p, start, n * 4, cudaMemcpyHostToDevice), "known-site upload");
+        CK(cudaMemcpy(p + n, stop, n * 4, cudaMemcpyHostToDevice), "known-site upload");
+        CK(cudaMemcpy(p + 2 * size_t(n), maxend.data(), n * 4, cudaMemcpyHostToDevice), "known-site upload");
+    }
+    eng->h_sites[id] = DevSites{p, p + n, p + 2 * size_t(n), n, 0};
+    return upload_refs(eng);
+}
+
+static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device);
+
+fp_status fp_engine_submit_batch(fp_engine *eng, const fp_batch_view *v) { return submit(eng, v, false); }
+
+fp_status fp_engine_submit_batch_device(fp_engine *eng, const fp_batch_view *v) { return submit(eng, v, true); }
+
+void *fp_engine_cuda_stream(fp_engine *eng) { return eng ? reinterpret_cast<void *>(eng->st) : nullptr; }
+
+static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) {
+    if (!eng || !v) return FP_BAD_INPUT;
+    if (eng->finalized) return eng->fail(FP_NOT_READY, "submit after finalize; call fp_engine_reset first");
+    CK(cudaSetDevice(eng->device), "set device");
+    cudaStream_t st = eng->st;
+    const uint32_t R = v->num_reads;
+    const uint64_t Q = v->num_qualities;
+    const uint32_t C = v->num_cigar_ops;
+    const uint64_t W = (v->num_read_symbols + 7) / 8;
+    if (R == 0) {
+        eng->stats.num_batches++;
+        return FP_OK;
+    }
+    const void *arrays[] = {v->chromosome, v->alignment_start, v->alignment_stop, v->mate_alignment_start,
+                            v->inferred_insert_size, v->cigars, v->cigar_start, v->cigar_len, v->reads,
+                            v->read_start, v->read_len, v->qualities, v->qual_start, v->qual_len, v->flags, v->mapq,
+                            v->read_group};
+    const size_t sizes[] = {R * 2ull, R * 4ull, R * 4ull, R * 4ull, R * 4ull, C * 4ull, R * 4ull, R * 4ull, W * 4,
+                            R * 4ull, R * 4ull, Q, R * 4ull, R * 4ull, R * 2ull, R * 1ull, R * 4ull};
+    for (int i = 0; i < 17; i++)
+        if (!arrays[i] && sizes[i]) return eng->fail(FP_BAD_INPUT, "null batch array");
+
+    cudaEventRecord(eng->ev[0], st);
+    // ---- inputs ----
+    size_t total = 0;
+    size_t offs[17];
+    for (int i = 0; i < 17; i++) {
+        offs[i] = total;
+        total += al(sizes[i] ? sizes[i] : 1);
+    }
+    char *base = nullptr;
+    if (on_device) {
+        // arrays are device pointers already: address them relative to a null base
+        for (int i = 0; i < 17; i++) offs[i] = size_t(reinterpret_cast<uintptr_t>(arrays[i]));
+    } else {
+        CK(eng->in_buf.ensure(total), "batch input allocation");
+        base = eng->in_buf.as<char>();
+        for (int i = 0; i < 17; i++)
+            if (sizes[i]) CK(cudaMemcpyAsync(base + offs[i], arrays[i], sizes[i], cudaMemcpyHostToDevice, st), "H2D");
+    }
+    DevBatch &b = eng->batch;
+    b.R = R;
+    b.num_cigar_ops = C;
+    b.num_syms = v->num_read_symbols;
+    b.num_quals = Q;
+    b.chromosome = reinterpret_cast<const u16 *>(base + offs[0]);
+    b.astart = reinterpret_cast<const u32 *>(base + offs[1]);
+    b.astop = reinterpret_cast<const u32 *>(base + offs[2]);
+    b.mstart = reinterpret_cast<const u32 *>(base + offs[3]);
+    b.isize = reinterpret_cast<const i32 *>(base + offs[4]);
+    b.cigars = reinterpret_cast<const u32 *>(base + offs[5]);
+    b.cigar_start = reinterpret_cast<const u32 *>(base + offs[6]);
+    b.cigar_len = reinterpret_cast<const u32 *>(base + offs[7]);
+    b.reads = reinterpret_cast<const u32 *>(base + offs[8]);
+    b.read_start = reinterpret_cast<const u32 *>(base + offs[9]);
+    b.read_len = reinterpret_cast<const u32 *>(base + offs[10]);
+    b.quals = reinterpret_cast<const u8 *>(base + offs[11]);
+    b.qual_start = reinterpret_cast<const u32 *>(base + offs[12]);
+    b.qual_len = reinterpret_cast<const u32 *>(base + offs[13]);
+    b.flags = reinterpret_cast<const u16 *>(base + offs[14]);
+    b.mapq = reinterpret_cast<const u8 *>(base + offs[15]);
+    b.rg = reinterpret_cast<const u32 *>(base + offs[16]);
+    cudaEventRecord(eng->ev[1], st);
+
+    // ---- validation + CIGAR-length scan ----
+    BatchWork &w = eng->work;
+    CK(eng->counters.ensure(64 * sizeof(u32)), "counters");
+    w.counters = eng->counters.as<u32>();
+    w.err = w.counters + 32;
+    CK(cudaMemsetAsync(w.counters, 0, 64 * sizeof(u32), st), "counters");
+    CK(eng->oplen.ensure(al((C + 1) * 4ull)), "op lengths");
+    CK(eng->cigoff.ensure(al((C + 1) * 4ull)), "cigar offsets");
+    const size_t scan_need = std::max(scan_tmp_bytes(C + 1), scan_tmp_bytes(R + 1));
+    CK(eng->scan_tmp.ensure(scan_need), "scan scratch");
+    launch_validate(b, eng->n_rg, w.err, st);
+    launch_op_lengths(b, eng->oplen.as<u32>(), st);
+    w.cigar_offsets = eng->cigoff.as<u32>();
+    launch_exclusive_scan(eng->oplen.as<u32>(), w.cigar_offsets, C, eng->scan_tmp.p, st);
+    u32 hdr[2] = {0, 0};
+    CK(cudaMemcpyAsync(&hdr[0], w.err, 4, cudaMemcpyDeviceToHost, st), "D2H");
+    CK(cudaMemcpyAsync(&hdr[1], w.cigar_offsets + C, 4, cudaMemcpyDeviceToHost, st), "D2H");
+    CK(cudaStreamSynchronize(st), "validation");
+    if (hdr[0]) {
+        std::string m = "batch rejected:";
+        if (hdr[0] & ERR_BAD_READ_RANGE) m += " read/cigar/quality range outside the batch arrays;";
+        if (hdr[0] & ERR_READ_TOO_LONG) m += " read longer than 511 bases (10-bit cycle covariate);";
+        if (hdr[0] & ERR_BAD_READ_GROUP) m += " read group id >= num_read_groups;";
+        return eng->fail(FP_BAD_INPUT, m);
+    }
+    const u64 E = hdr[1];
+
+    // ---- work arrays ----
+    CK(eng->ev_rc.ensure(al(E * 4 + 4)), "events");
+    CK(eng->ev_type.ensure(al(E + 4)), "events");
+    w.ev_rc = eng->ev_rc.as<u32>();
+    w.ev_type = eng->ev_type.as<u8>();
+    w.num_events = E;
+    const size_t pr_bytes = al(R) + al(R * 16ull) + al(R * 4ull) + al(R * 2ull) + al(R * 2ull);
+    CK(eng->per_read.ensure(pr_bytes), "per-read arrays");
+    {
+        char *p = eng->per_read.as<char>();
+        w.status = reinterpret_cast<u8 *>(p); p += al(R);
+        w.win = reinterpret_cast<u16 *>(p); p += al(R * 16ull);
+        w.hmm = reinterpret_cast<i16 *>(p); p += al(R * 4ull);
+        w.bw = reinterpret_cast<u16 *>(p); p += al(R * 2ull);
+        w.nerr = reinterpret_cast<u16 *>(p);
+    }
+    const size_t pb_bytes = al(Q) * 4 + al(Q * 4) + al(Q * 12);
+    CK(eng->per_base.ensure(pb_bytes), "per-base arrays");
+    {
+        char *p = eng->per_base.as<char>();
+        w.bflags = reinterpret_cast<u8 *>(p); p += al(Q);
+        w.tag = reinterpret_cast<u8 *>(p); p += al(Q);
+        w.baq_q = reinterpret_cast<u8 *>(p); p += al(Q);
+        w.baq_amb = reinterpret_cast<u8 *>(p); p += al(Q);
+        w.baq_state = reinterpret_cast<u32 *>(p); p += al(Q * 4);
+        w.frac = reinterpret_cast<float *>(p);
+    }
+    CK(eng->lists.ensure(al(R * 4ull) * 4), "work lists");
+    w.baq_list = eng->lists.as<u32>();
+    w.esc_list = w.baq_list + 3ull * R;
+    CK(eng->entry_cnt.ensure(al((R + 1) * 4ull)), "entry counts");
+    CK(eng->entry_off.ensure(al((R + 1) * 4ull)), "entry offsets");
+    w.entry_count = eng->entry_cnt.as<u32>();
+    w.entry_offset = eng->entry_off.as<u32>();
+    CK(cudaMemsetAsync(w.tag, 0xFF, Q, st), "tag init");
+    cudaEventRecord(eng->ev[2], st);
+
+    // ---- K1 ----
+    launch_prep(b, eng->ref, w, st);
+    cudaEventRecord(eng->ev[3], st);
+    u32 cnt[16];
+    CK(cudaMemcpyAsync(cnt, w.counters, sizeof(cnt), cudaMemcpyDeviceToHost, st), "D2H");
+    CK(cudaStreamSynchronize(st), "prep");
+    const u32 bw_max[3] = {cnt[12], cnt[13], cnt[14]};
+    const u32 n_cls[3] = {cnt[0], cnt[1], cnt[2]};
+
+    // ---- K2 BAQ ----
+    const uint32_t max_q = cnt[7] ? cnt[7] : 1;  // longest BAQ query window of the batch
+    auto run_fp64 = [&](const u32 *list, const u32 *count, u32 nmax, u32 max_bw) -> fp_status {
+        if (!nmax) return FP_OK;
+        const u32 threads = std::min<u32>(baq64_threads(), ((nmax + 127) / 128) * 128);
+        u64 need = baq64_scratch_doubles(threads, max_q, max_bw);
+        const u64 budget = (u64(6) << 30) / 8;  // at most 6 GiB of FP64 scratch
+        if (need > budget) need = std::max<u64>(budget, baq64_scratch_doubles(128, max_q, max_bw));
+        CK(eng->s64.ensure(need * 8), "FP64 BAQ scratch");
+        eng->s64_doubles = eng->s64.cap / 8;
+        launch_baq64(b, eng->ref, w, list, count, nmax, eng->s64.as<double>(), eng->s64_doubles, max_q, max_bw, st);
+        launch_cap(b, w, list, count, 1, st, nmax);
+        return FP_OK;
+    };
+    fp_status s;
+    if (eng->baq_mode == FP_BAQ_FP64) {
+        for (int c = 0; c < 3; c++) {
+            if ((s = run_fp64(w.baq_list + size_t(c) * R, w.counters + c, n_cls[c], bw_max[c])) != FP_OK) return s;
+        }
+    } else {
+        const u64 s32_need = std::max(baq32_scratch_floats(16, 512), baq32_scratch_floats(32, 512));
+        CK(eng->s32.ensure(s32_need * 4), "FP32 BAQ scratch");
+        if (n_cls[0]) launch_baq32(b, eng->ref, w, w.baq_list, w.counters + 0, n_cls[0], 16, eng->s32.as<float>(), 512, st);
+        if (n_cls[1])
+            launch_baq32(b, eng->ref, w, w.baq_list + size_t(R), w.counters + 1, n_cls[1], 32, eng->s32.as<float>(), 512, st);
+        if (n_cls[0]) launch_cap(b, w, w.baq_list, w.counters + 0, 0, st, n_cls[0]);
+        if (n_cls[1]) launch_cap(b, w, w.baq_list + size_t(R), w.counters + 1, 0, st, n_cls[1]);
+        if ((s = run_fp64(w.baq_list + 2ull * R, w.counters + 2, n_cls[2], bw_max[2])) != FP_OK) return s;
+        // escalated reads (at most the class 0 and 1 reads)
+        if ((s = run_fp64(w.esc_list, w.counters + 4, n_cls[0] + n_cls[1], std::max(bw_max[0], bw_max[1]))) != FP_OK)
+            return s;
+    }
+    cudaEventRecord(eng->ev[4], st);
+
+    // ---- K3 count + scan ----
+    launch_cov_count(b, w, eng->tables, st);
+    launch_exclusive_scan(w.entry_count, w.entry_offset, R, eng->scan_tmp.p, st);
+    u32 tail[2];
+    CK(cudaMemcpyAsync(&tail[0], w.entry_offset + R, 4, cudaMemcpyDeviceToHost, st), "D2H");
+    CK(cudaMemcpyAsync(&tail[1], w.counters + 4, 4, cudaMemcpyDeviceToHost, st), "D2H");
+    CK(cudaStreamSynchronize(st), "covariates");
+    const u64 N = tail[0];
+    CK(eng->entries.ensure(al(N * 8 + 8)), "entries");
+    CK(eng->entries_alt.ensure(al(N * 8 + 8)), "entries");
+    w.entries = eng->entries.as<u64>();
+    w.entries_alt = eng->entries_alt.as<u64>();
+    CK(eng->sort_tmp.ensure(std::max(radix_tmp_bytes(N), fold_tmp_bytes(N))), "sort scratch");
+    launch_cov_emit(b, w, eng->tables, st);
+    cudaEventRecord(eng->ev[5], st);
+
+    // ---- K4 sort + ordered fold ----
+    int key_bits = 1;
+    while (key_bits < 32 && (1ull << key_bits) < eng->tables.ks.total) key_bits++;
+    u64 *sorted = w.entries;
+    launch_radix_sort(w.entries, w.entries_alt, N, key_bits, eng->sort_tmp.p, eng->sort_tmp.cap, &sorted, st);
+    launch_fold(sorted, N, eng->tables.mism, eng->sort_tmp.p, st);
+    cudaEventRecord(eng->ev[6], st);
+    u32 dev_err = 0;
+    CK(cudaMemcpyAsync(cnt, w.counters, sizeof(cnt), cudaMemcpyDeviceToHost, st), "D2H");
+    CK(cudaMemcpyAsync(&dev_err, w.err, 4, cudaMemcpyDeviceToHost, st), "D2H");
+    CK(cudaStreamSynchronize(st), "batch");
+    if (dev_err & (ERR_INTERNAL | ERR_TIMEOUT | ERR_CAPACITY))
+        return eng->fail(FP_DEVICE_ERROR, "kernel reported an internal error status");
+    float ms;
+    const int stage_of[6] = {FP_STAGE_H2D, FP_STAGE_OTHER, FP_STAGE_PREP, FP_STAGE_BAQ, FP_STAGE_COVARIATES,
+                             FP_STAGE_SORT_REDUCE};
+    for (int i = 0; i < 6; i++) {
+        if (cudaEventElapsedTime(&ms, eng->ev[i], eng->ev[i + 1]) == cudaSuccess)
+            eng->stats.gpu_ms_per_stage[stage_of[i]] += ms;
+    }
+    eng->stats.total_reads += R;
+    eng->stats.filtered_reads += cnt[5];
+    eng->stats.baq_reads += cnt[6];
+    eng->stats.baq_fp64_escalated_reads += tail[1];
+    eng->stats.num_batches++;
+    eng->last_R = R;
+    eng->last_Q = Q;
+    return FP_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+fp_status fp_engine_finalize(fp_engine *eng) {
+    if (!eng) return FP_BAD_INPUT;
+    CK(cudaSetDevice(eng->device), "set device");
+    cudaStream_t st = eng->st;
+    cudaEventRecord(eng->ev[7], st);
+    const KeySpace ks = eng->tables.ks;
+    const u32 T = ks.total;
+    DevBuf flags, pos, rows, rkey, robs, rmism, rexp, rest, rcoef, remp, rg, tmp;
+    auto cleanup = [&]() {
+        DevBuf *bs[] = {&flags, &pos, &rows, &rkey, &robs, &rmism, &rexp, &rest, &rcoef, &remp, &rg, &tmp};
+        for (DevBuf *x : bs) x->release();
+    };
+    auto bail = [&](cudaError_t e, const char *w) {
+        cleanup();
+        return eng->cuda_fail(e, w);
+    };
+#define CKF(call, where)                          \
+    do {                                          \
+        cudaError_t _e = (call);                  \
+        if (_e != cudaSuccess) return bail(_e, where); \
+    } while (0)
+    CKF(flags.ensure(al(T * 4ull + 4)), "finalize");
+    CKF(pos.ensure(al(T * 4ull + 8)), "finalize");
+    CKF(tmp.ensure(scan_tmp_bytes(T)), "finalize");
+    launch_mark_nonzero(eng->tables, flags.as<u32>(), st);
+    launch_exclusive_scan(flags.as<u32>(), pos.as<u32>(), T, tmp.p, st);
+    u32 nrows = 0;
+    CKF(cudaMemcpyAsync(&nrows, pos.as<u32>() + T, 4, cudaMemcpyDeviceToHost, st), "finalize");
+    CKF(cudaStreamSynchronize(st), "finalize");
+    const size_t n = std::max<u32>(nrows, 1);
+    CKF(rows.ensure(n * 4), "finalize");
+    CKF(rkey.ensure(n * 4), "finalize");
+    CKF(robs.ensure(n * 8), "finalize");
+    CKF(rmism.ensure(n * 8), "finalize");
+    CKF(rexp.ensure(n * 8), "finalize");
+    CKF(rest.ensure(n * 8), "finalize");
+    CKF(rcoef.ensure((n + 768) * 8), "finalize");
+    CKF(remp.ensure((n + 768) * 8), "finalize");
+    CKF(rg.ensure(768 * 8 * 3 + 768 * 8 * 3), "finalize");
+    launch_gather_rows(eng->tables, flags.as<u32>(), pos.as<u32>(), rows.as<u32>(), st);
+    launch_rows(eng->tables, rows.as<u32>(), nrows, rkey.as<u32>(), robs.as<u64>(), rmism.as<double>(),
+                rexp.as<double>(), rest.as<double>(), st);
+    u64 *rg_obs = rg.as<u64>();
+    double *rg_mism = reinterpret_cast<double *>(rg_obs + 768);
+    double *rg_exp = rg_mism + 768;
+    launch_rg_fold(eng->tables, rg_obs, rg_mism, rg_exp, st);
+
+    std::vector<u32> key(nrows), dense(nrows);
+    std::vector<u64> obs(nrows);
+    std::vector<double> mism(nrows), ex(nrows), est(nrows);
+    const u32 ng = ks.n_rg * 3;
+    std::vector<u64> g_obs(ng);
+    std::vector<double> g_mism(ng), g_exp(ng);
+    if (nrows) {
+        CKF(cudaMemcpyAsync(key.data(), rkey.p, nrows * 4ull, cudaMemcpyDeviceToHost, st), "finalize");
+        CKF(cudaMemcpyAsync(dense.data(), rows.p, nrows * 4ull, cudaMemcpyDeviceToHost, st), "finalize");
+        CKF(cudaMemcpyAsync(obs.data(), robs.p, nrows * 8ull, cudaMemcpyDeviceToHost, st), "finalize");
+        CKF(cudaMemcpyAsync(mism.data(), rmism.p, nrows * 8ull, cudaMemcpyDeviceToHost, st), "finalize");
+        CKF(cudaMemcpyAsync(ex.data(), rexp.p, nrows * 8ull, cudaMemcpyDeviceToHost, st), "finalize");
+        CKF(cudaMemcpyAsync(est.data(), rest.p, nrows * 8ull, cudaMemcpyDeviceToHost, st), "finalize");
+    }
+    CKF(cudaMemcpyAsync(g_obs.data(), rg_obs, ng * 8ull, cudaMemcpyDeviceToHost, st), "finalize");
+    CKF(cudaMemcpyAsync(g_mism.data(), rg_mism, ng * 8ull, cudaMemcpyDeviceToHost, st), "finalize");
+    CKF(cudaMemcpyAsync(g_exp.data(), rg_exp, ng * 8ull, cudaMemcpyDeviceToHost, st), "finalize");
+    CKF(cudaStreamSynchronize(st), "finalize");
+
+    // read-group rows (keys rg<<10 | ev) and the host libm values of the empirical-quality model
+    std::vector<u32> gkey;
+    std::vector<u64> gobs;
+    std::vector<double> gmism, gexp, gest;
+    for (u32 i = 0; i < ng; i++) {
+        if (!g_obs[i]) continue;
+        gkey.push_back(((i / 3) << 10) | (i % 3));
+        gobs.push_back(g_obs[i]);
+        gmism.push_back(g_mism[i]);
+        gexp.push_back(g_exp[i]);
+        gest.push_back(double(-10.0 * log10(g_exp[i] / double(g_obs[i]))));
+    }
+    const u32 ngr = u32(gkey.size());
+    std::vector<double> coef(size_t(nrows) + ngr);
+    for (u32 i = 0; i < nrows; i++) coef[i] = binomial_coef(obs[i], mism[i]);
+    for (u32 i = 0; i < ngr; i++) coef[size_t(nrows) + i] = binomial_coef(gobs[i], gmism[i]);
+
+    // empirical qualities: table rows (rounded prior) and read-group rows (truncated prior)
+    double *d_coef = rcoef.as<double>();
+    double *d_emp = remp.as<double>();
+    if (nrows + ngr)
+        CKF(cudaMemcpyAsync(d_coef, coef.data(), (size_t(nrows) + ngr) * 8, cudaMemcpyHostToDevice, st), "finalize");
+    launch_empirical(nrows, robs.as<u64>(), rmism.as<double>(), rest.as<double>(), d_coef, 1, d_emp, st);
+    DevBuf gb;
+    if (ngr) {
+        CKF(gb.ensure(ngr * 24ull), "finalize");
+        u64 *gdo = gb.as<u64>();
+        double *gdm = reinterpret_cast<double *>(gdo + ngr);
+        double *gde = gdm + ngr;
+        CKF(cudaMemcpyAsync(gdo, gobs.data(), ngr * 8ull, cudaMemcpyHostToDevice, st), "finalize");
+        CKF(cudaMemcpyAsync(gdm, gmism.data(), ngr * 8ull, cudaMemcpyHostToDevice, st), "finalize");
+        CKF(cudaMemcpyAsync(gde, gest.data(), ngr * 8ull, cudaMemcpyHostToDevice, st), "finalize");
+        launch_empirical(ngr, gdo, gdm, gde, d_coef + nrows, 0, d_emp + nrows, st);
+    }
+    std::vector<double> emp(size_t(nrows) + ngr);
+    if (nrows + ngr)
+        CKF(cudaMemcpyAsync(emp.data(), d_emp, (size_t(nrows) + ngr) * 8, cudaMemcpyDeviceToHost, st), "finalize");
+    cudaEventRecord(eng->ev[8], st);
+    CKF(cudaStreamSynchronize(st), "finalize");
+    gb.release();
+    cleanup();
+#undef CKF
+
+    for (auto &t : eng->out) t = HostTable();
+    HostTable &tg = eng->out[FP_TABLE_READ_GROUP];
+    tg.keys = gkey;
+    tg.obs = gobs;
+    tg.mism = gmism;
+    tg.exp = gexp;
+    tg.est = gest;
+    tg.emp.assign(emp.begin() + nrows, emp.end());
+    // rows ascend in dense index: quality rows, then cycle rows, then context rows (the dense ranges are
+    // ordered), so the table of a row follows from its dense index
+    for (u32 i = 0; i < nrows; i++) {
+        const u32 d = dense[i];
+        const int t = d < ks.cycle_base ? FP_TABLE_QUALITY : (d < ks.context_base ? FP_TABLE_CYCLE : FP_TABLE_CONTEXT);
+        HostTable &h = eng->out[t];
+        h.keys.push_back(key[i]);
+        h.obs.push_back(obs[i]);
+        h.mism.push_back(mism[i]);
+        h.exp.push_back(ex[i]);
+        h.est.push_back(est[i]);
+        h.emp.push_back(emp[i]);
+    }
+    float ms;
+    if (cudaEventElapsedTime(&ms, eng->ev[7], eng->ev[8]) == cudaSuccess)
+        eng->stats.gpu_ms_per_stage[FP_STAGE_POSTPROCESS] += ms;
+    eng->finalized = true;
+    return FP_OK;
+}
+
+fp_status fp_engine_get_table(fp_engine *eng, int32_t id, fp_table_view *out) {
+    if (!eng || !out || id < 0 || id > 3) return FP_BAD_INPUT;
+    if (!eng->finalized) return eng->fail(FP_NOT_READY, "tables are available after fp_engine_finalize");
+    const HostTable &h = eng->out[id];
+    out->num_rows = uint32_t(h.keys.size());
+    out->keys = h.keys.data();
+    out->observations = h.obs.data();
+    out->mismatches = h.mism.data();
+    out->expected_errors = h.exp.data();
+    out->estimated_quality = h.est.data();
+    out->empirical_quality = h.emp.data();
+    return FP_OK;
+}
+
+fp_status fp_engine_write_report(fp_engine *eng, const char *path, const char *const *rg_names, uint32_t num_rg_names,
+                                 int disable_rounding, int vmaj, int vmin, int vrev) {
+    if (!eng) return FP_BAD_INPUT;
+    if (!eng->finalized) return eng->fail(FP_NOT_READY, "write_report needs fp_engine_finalize first");
+    fp_table_view t[4];
+    for (int i = 0; i < 4; i++) fp_engine_get_table(eng, i, &t[i]);
+    const fp_status s = fp_report_write(path, t, rg_names, num_rg_names, disable_rounding, vmaj, vmin, vrev);
+    if (s != FP_OK) eng->err = "cannot open report output";
+    return s;
+}
+
+fp_status fp_engine_reset(fp_engine *eng) {
+    if (!eng) return FP_BAD_INPUT;
+    CK(cudaSetDevice(eng->device), "set device");
+    const size_t n = eng->tables.ks.total;
+    CK(cudaMemsetAsync(eng->tab_obs.p, 0, n * sizeof(unsigned long long), eng->st), "reset");
+    CK(cudaMemsetAsync(eng->tab_mism.p, 0, n * sizeof(float), eng->st), "reset");
+    CK(cudaStreamSynchronize(eng->st), "reset");
+    for (auto &t : eng->out) t = HostTable();
+    eng->finalized = false;
+    eng->stats = fp_stats{};
+    eng->launch_base = g_kernel_launches;
+    return FP_OK;
+}
+
+fp_status fp_engine_get_stats(const fp_engine *eng, fp_stats *out) {
+    if (!eng || !out) return FP_BAD_INPUT;
+    *out = eng->stats;
+    out->gpu_kernel_launches = g_kernel_launches - eng->launch_base;
+    return FP_OK;
+}
+
+fp_status fp_engine_debug_last_batch(fp_engine *eng, uint8_t *read_status, uint16_t *windows, int16_t *hmm,
+                                     uint8_t *base_flags, uint8_t *baq_tag, double *frac_errors) {
+    if (!eng) return FP_BAD_INPUT;
+    CK(cudaSetDevice(eng->device), "set device");
+    CK(cudaStreamSynchronize(eng->st), "debug");
+    const uint32_t R = eng->last_R;
+    const uint64_t Q = eng->last_Q;
+    const BatchWork &w = eng->work;
+    if (read_status) CK(cudaMemcpy(read_status, w.status, R, cudaMemcpyDeviceToHost), "debug");
+    if (windows) CK(cudaMemcpy(windows, w.win, R * 16ull, cudaMemcpyDeviceToHost), "debug");
+    if (hmm) {
+        std::vector<int16_t> hw(size_t(R) * 2);
+        std::vector<uint16_t> bw(R), ne(R);
+        CK(cudaMemcpy(hw.data(), w.hmm, R * 4ull, cudaMemcpyDeviceToHost), "debug");
+        CK(cudaMemcpy(bw.data(), w.bw, R * 2ull, cudaMemcpyDeviceToHost), "debug");
+        CK(cudaMemcpy(ne.data(), w.nerr, R * 2ull, cudaMemcpyDeviceToHost), "debug");
+        for (uint32_t r = 0; r < R; r++) {
+            hmm[r * 4 + 0] = hw[r * 2];
+            hmm[r * 4 + 1] = hw[r * 2 + 1];
+            hmm[r * 4 + 2] = int16_t(bw[r]);
+            hmm[r * 4 + 3] = int16_t(ne[r]);
+        }
+    }
+    if (base_flags) CK(cudaMemcpy(base_flags, w.bflags, Q, cudaMemcpyDeviceToHost), "debug");
+    if (baq_tag) CK(cudaMemcpy(baq_tag, w.tag, Q, cudaMemcpyDeviceToHost), "debug");
+    if (frac_errors) {
+        std::vector<float> f(Q * 3);
+        CK(cudaMemcpy(f.data(), w.frac, Q * 12, cudaMemcpyDeviceToHost), "debug");
+        for (uint64_t i = 0; i < Q * 3; i++) frac_errors[i] = f[i];
+    }
+    return FP_OK;
+}
+
+fp_status fp_host_alloc(size_t bytes, void **out) {
+    if (!out) return FP_BAD_INPUT;
+    return cudaMallocHost(out, bytes ? bytes : 1) == cudaSuccess ? FP_OK : FP_OOM;
+}
+
+void fp_host_free(void *p) {
+    if (p) cudaFreeHost(p);
+}
+
+}  // extern "C"

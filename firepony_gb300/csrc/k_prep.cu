@@ -1,0 +1,729 @@
+// K1 read preparation: input validation, read filters, CIGAR expansion, clipping windows, error vectors,
+// base and known-site masks and the BAQ work list — one thread per read, every stage of the reference's
+// per-read functors fused into one pass over the read's events (which stay in L1/L2 while it runs).
+// K2b (BAQ capping and BQ-tag encoding) is also here because it walks the same events.
+#include "kernels.h"
+
+namespace fpg {
+
+unsigned long long g_kernel_launches = 0;
+
+namespace {
+
+struct us2 { u16 x, y; };
+struct ss2 { i16 x, y; };
+
+template <typename T> __device__ __forceinline__ T tmin(T a, T b) { return a < b ? a : b; }
+template <typename T> __device__ __forceinline__ T tmax(T a, T b) { return a > b ? a : b; }
+__device__ __forceinline__ u32 baq_abs(i32 v) { return v < 0 ? u32(-v) : u32(v); }  // device/baq.cu:84-87
+
+// ---------------------------------------------------------------------------------------------------
+// validation: ranges in bounds, read length <= 511, read group < n_rg (or none)
+__global__ void k_validate(DevBatch b, u32 n_rg, u32 *err) {
+    const u32 r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= b.R) return;
+    u32 e = 0;
+    if (u64(b.cigar_start[r]) + b.cigar_len[r] > b.num_cigar_ops) e |= ERR_BAD_READ_RANGE;
+    if (u64(b.read_start[r]) + b.read_len[r] > b.num_syms) e |= ERR_BAD_READ_RANGE;
+    if (u64(b.qual_start[r]) + b.qual_len[r] > b.num_quals) e |= ERR_BAD_READ_RANGE;
+    if (b.read_len[r] > MAX_READ_LEN) e |= ERR_READ_TOO_LONG;
+    if (b.rg[r] != U32_NONE && b.rg[r] >= n_rg) e |= ERR_BAD_READ_GROUP;
+    if (e) raise_error(err, e);
+}
+
+__global__ void k_op_lengths(DevBatch b, u32 *out) {
+    const u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < b.num_cigar_ops) out[i] = op_len(b.cigars[i]);
+}
+
+// ---------------------------------------------------------------------------------------------------
+struct Read {
+    const DevBatch &b;
+    const DevRef &ref;
+    const BatchWork &w;
+    u32 r;
+    u32 cs, ce;         // event range (global event indices)
+    u32 *rc;            // ev_rc + cs
+    u8 *ty;             // ev_type + cs
+    u32 n;              // events in the read
+    u32 qs, rs, rlen;
+    u32 astart;
+    u16 flags;
+
+    __device__ Read(const DevBatch &b_, const DevRef &ref_, const BatchWork &w_, u32 r_) : b(b_), ref(ref_), w(w_), r(r_) {
+        cs = w.cigar_offsets[b.cigar_start[r]];
+        ce = w.cigar_offsets[b.cigar_start[r] + b.cigar_len[r]];
+        rc = w.ev_rc + cs;
+        ty = w.ev_type + cs;
+        n = ce - cs;
+        qs = b.qual_start[r];
+        rs = b.read_start[r];
+        rlen = b.read_len[r];
+        astart = b.astart[r];
+        flags = b.flags[r];
+    }
+    __device__ __forceinline__ u16 readc(u32 e) const { return u16(rc[e] & 0xFFFF); }
+    __device__ __forceinline__ u16 refc(u32 e) const { return u16(rc[e] >> 16); }
+    __device__ __forceinline__ u8 sym(u32 i) const { return sym4(b.reads, u64(rs) + i); }
+};
+
+__device__ const DevContig *contig_of(const DevRef &ref, u32 id) {
+    if (id < ref.num_contigs && ref.contigs[id].size > 0) return &ref.contigs[id];
+    return nullptr;
+}
+
+// filter_mapq, filter_if_any_set, filter_if_cigar_malformed (device/read_filters.cu:42-75, :156-258)
+__device__ bool passes_invalid_filters(const DevBatch &b, u32 r) {
+    if (b.mapq[r] == 0 || b.mapq[r] == 255) return false;
+    if (b.flags[r] & (F_DUPLICATE | F_QC_FAIL | F_UNMAP | F_SECONDARY)) return false;
+    int st = 0;  // 0 leading hard, 1 leading soft, 2 no clips, 3 trailing soft, 4 trailing hard
+    const u32 c0 = b.cigar_start[r], c1 = c0 + b.cigar_len[r];
+    for (u32 i = c0; i < c1; i++) {
+        const u32 op = op_code(b.cigars[i]);
+        if (op == OP_N) return false;
+        if (op == OP_H) {
+            if (st == 1) return false;
+            if (st == 2 || st == 3) st = 4;
+        } else if (op == OP_S) {
+            if (st == 0) st = 1;
+            else if (st == 2) st = 3;
+            else if (st == 4) return false;
+        } else {
+            if (st == 0 || st == 1) st = 2;
+            else if (st == 3 || st == 4) return false;
+        }
+    }
+    return true;
+}
+
+// compute_read_offset_list + compute_alignment_window (device/snp_filter.cu:42-147): the window ends at the
+// reference offset of the last read base that has one. Also returns the number of read bases the CIGAR
+// covers and whether an op code above X occurs.
+__device__ void alignment_window(const DevBatch &b, u32 r, u32 &wx, u32 &wy, u32 &covered, bool &bad_op) {
+    u16 offset = 0;
+    u32 pos = 0;
+    int last = -1;
+    u16 last_off = 0;
+    bad_op = false;
+    const u32 c0 = b.cigar_start[r], c1 = c0 + b.cigar_len[r];
+    const u32 rlen = b.read_len[r];
+    for (u32 c = c0; c < c1; c++) {
+        const u32 v = b.cigars[c], op = op_code(v), len = op_len(v);
+        switch (op) {
+        case OP_M: case OP_EQ: case OP_X:
+            if (len) {
+                // offsets offset .. offset+len-1 at read positions pos .. pos+len-1
+                u32 lastpos = pos + len - 1;
+                if (pos < rlen) {
+                    u32 lp = lastpos < rlen ? lastpos : rlen - 1;
+                    last = int(lp);
+                    last_off = u16(offset + (lp - pos));
+                }
+                offset = u16(offset + len);
+                pos += len;
+            }
+            break;
+        case OP_I: case OP_N:
+            if (len) {
+                u32 lastpos = pos + len - 1;
+                if (pos < rlen) {
+                    u32 lp = lastpos < rlen ? lastpos : rlen - 1;
+                    last = int(lp);
+                    last_off = offset;
+                }
+                pos += len;
+            }
+            break;
+        case OP_D: case OP_H: case OP_P:
+            offset = u16(offset + len);
+            break;
+        case OP_S:
+            pos += len;
+            break;
+        default:
+            bad_op = true;
+            break;
+        }
+    }
+    covered = pos;
+    if (last < 0) {
+        wx = U32_NONE;
+        wy = U32_NONE;
+    } else {
+        wx = b.astart[r];
+        wy = b.astart[r] + last_off;
+    }
+}
+
+// cigar_coordinates_expand (device/cigar.cu:536-614) + cigar_op_expand (:55-95)
+__device__ void expand_read(Read &rd) {
+    const DevBatch &b = rd.b;
+    u16 ro = 0, fo = 0;
+    u32 e = 0;
+    const u32 c0 = b.cigar_start[rd.r], c1 = c0 + b.cigar_len[rd.r];
+    for (u32 c = c0; c < c1; c++) {
+        const u32 v = b.cigars[c], op = op_code(v), len = op_len(v);
+        for (u32 i = 0; i < len; i++, e++) {
+            u32 rc;
+            u8 t;
+            switch (op) {
+            case OP_M: case OP_EQ: case OP_X: rc = u32(ro++) | (u32(fo++) << 16); t = EV_M; break;
+            case OP_S: rc = u32(ro++) | (u32(U16_NONE) << 16); t = EV_S; break;
+            case OP_N: case OP_I: rc = u32(ro++) | (u32(U16_NONE) << 16); t = EV_I; break;
+            default: rc = u32(U16_NONE) | (u32(fo++) << 16); t = EV_D; break;  // D, H, P
+            }
+            rd.rc[e] = rc;
+            rd.ty[e] = t;
+        }
+    }
+}
+
+// remove_adapters (device/cigar.cu:111-344). The backward walk for a left tail cannot leave the read: a
+// matched event without a read coordinate always follows the read's first read-coordinate event, because
+// the window check before it rejects boundaries left of the first aligned base.
+__device__ int read_coord_for_ref(const Read &rd, u32 ref_coord, bool right_tail) {
+    for (u32 ev = 0; ev < rd.n; ev++) {
+        if (rd.astart + u32(rd.refc(ev)) == ref_coord) {
+            u16 read_coord = rd.readc(ev);
+            if (read_coord == U16_NONE) {
+                if (right_tail) {
+                    while (ev < rd.n) {
+                        read_coord = rd.readc(ev);
+                        if (read_coord != U16_NONE) break;
+                        ev++;
+                    }
+                } else {
+                    while (ev > 0) {
+                        ev--;
+                        read_coord = rd.readc(ev);
+                        if (read_coord != U16_NONE) break;
+                    }
+                }
+                if (read_coord == U16_NONE) return -1;
+            }
+            return read_coord;
+        }
+    }
+    return -1;
+}
+
+__device__ us2 current_reference_window(const Read &rd, us2 w) {
+    us2 out = {0, 0};
+    for (u32 i = 0; i < rd.n; i++) {
+        if (rd.readc(i) == w.x) {
+            while (i < rd.n && rd.refc(i) == U16_NONE) i++;
+            if (i == rd.n) return us2{U16_NONE, U16_NONE};
+            out.x = rd.refc(i);
+            break;
+        }
+    }
+    for (int i = int(rd.n) - 1; i >= 0; i--) {
+        if (rd.readc(u32(i)) == w.y) {
+            while (rd.refc(u32(i)) == U16_NONE && i > 0) i--;
+            if (i == 0) return us2{U16_NONE, U16_NONE};
+            out.y = rd.refc(u32(i));
+            break;
+        }
+    }
+    return out;
+}
+
+__device__ void remove_adapters(const Read &rd, us2 &w) {
+    const DevBatch &b = rd.b;
+    const u32 r = rd.r;
+    const u32 flags = rd.flags;
+    const i32 isize = b.isize[r];
+    // hasWellDefinedFragmentSize (:117-146)
+    if (isize == 0) return;
+    if (!(flags & F_PAIRED)) return;
+    if ((flags & F_UNMAP) || (flags & F_MATE_UNMAP)) return;
+    const bool rev = flags & F_REVERSE, mate_rev = flags & F_MATE_REVERSE;
+    if (rev == mate_rev) return;
+    bool ok = rev ? (b.astop[r] > b.mstart[r]) : (rd.astart <= b.mstart[r] + u32(isize));
+    if (!ok) return;
+    // getAdaptorBoundary (:150-163)
+    u32 boundary;
+    if (rev) boundary = u32(b.mstart[r] - 1);
+    else boundary = u32(rd.astart + u32(isize < 0 ? -isize : isize) + 1u);
+    if (boundary == U32_NONE) return;
+    const us2 rw = current_reference_window(rd, w);
+    if (boundary < rd.astart + u32(rw.x) || boundary > rd.astart + u32(rw.y)) return;
+    if (rev) {
+        // hardClipByReferenceCoordinates with refStart = -1 (:251-266)
+        const int stop = read_coord_for_ref(rd, u32(int(boundary)), false);
+        w.x = tmax<u16>(w.x, u16(u16(stop) + 1));
+    } else {
+        int start;
+        if (int(boundary) < 0) start = 0;  // refStart < 0 branch
+        else start = read_coord_for_ref(rd, u32(int(boundary)), true);
+        w.y = tmin<u16>(w.y, u16(u16(start) - 1));
+    }
+}
+
+// remove_soft_clips (device/cigar.cu:346-408)
+__device__ void remove_soft_clips(const Read &rd, us2 &w) {
+    const DevBatch &b = rd.b;
+    const u32 c0 = b.cigar_start[rd.r], cl = b.cigar_len[rd.r];
+    u32 ci = c0, ro = 0;
+    while (ci < c0 + cl && ro < rd.rlen) {
+        const u32 v = b.cigars[ci], op = op_code(v), len = op_len(v);
+        if (op == OP_H || op == OP_S) {
+            if (ro + len > w.x) w.x = tmin<u16>(u16(ro + len), w.y);
+            ro += len;
+            ci++;
+        } else {
+            break;
+        }
+    }
+    if (cl > 0) {
+        int cj = int(c0 + cl - 1);
+        ro = rd.rlen - 1;
+        while (cj >= int(c0) && ro > w.x) {
+            const u32 v = b.cigars[cj], op = op_code(v), len = op_len(v);
+            if (op == OP_H || op == OP_S) {
+                if (ro - len < w.y) w.y = tmax<u16>(u16(ro - len), w.x);
+                ro -= len;
+                cj--;
+            } else {
+                break;
+            }
+        }
+    }
+}
+
+// compute_no_insertions_window (device/cigar.cu:410-471); (0xFFFF, 0xFFFF) when nothing qualifies
+__device__ us2 no_insertions_window(const Read &rd, us2 w) {
+    us2 out = {U16_NONE, U16_NONE};
+    for (u32 ev = 0; ev < rd.n; ev++) {
+        const u16 ro = rd.readc(ev);
+        if (ro == U16_NONE || ro < w.x) continue;
+        if (rd.ty[ev] == EV_I) continue;
+        out.x = ro;
+        break;
+    }
+    for (int ev = int(rd.n) - 1; ev >= 0; ev--) {
+        const u16 ro = rd.readc(u32(ev));
+        if (ro == U16_NONE || ro > w.y) continue;
+        if (rd.ty[ev] == EV_I) continue;
+        out.y = ro;
+        break;
+    }
+    return out;
+}
+
+// compute_reference_window (device/cigar.cu:473-534); same convention
+__device__ us2 reference_window(const Read &rd, us2 ni) {
+    us2 out = {U16_NONE, U16_NONE};
+    for (u32 i = 0; i < rd.n; i++) {
+        if (rd.readc(i) == ni.x) {
+            while (i < rd.n && rd.refc(i) == U16_NONE) i++;
+            if (i == rd.n) return us2{U16_NONE, U16_NONE};
+            out.x = rd.refc(i);
+            break;
+        }
+    }
+    for (int i = int(rd.n) - 1; i >= 0; i--) {
+        if (rd.readc(u32(i)) == ni.y) {
+            while (rd.refc(u32(i)) == U16_NONE && i > 0) i--;
+            if (i == 0) return us2{U16_NONE, U16_NONE};
+            out.y = rd.refc(u32(i));
+            break;
+        }
+    }
+    return out;
+}
+
+// compute_error_vectors (device/cigar.cu:616-737): only op codes M (0), I (1), D (2) count
+__device__ u16 error_vectors(const Read &rd, const DevContig *g, us2 w, us2 rw, u8 *bf) {
+    const DevBatch &b = rd.b;
+    const bool neg = rd.flags & F_REVERSE;
+    u16 cur = 0, nerr = 0;
+    const u32 c0 = b.cigar_start[rd.r], c1 = c0 + b.cigar_len[rd.r];
+    for (u32 c = c0; c < c1; c++) {
+        const u32 e0 = rd.w.cigar_offsets[c] - rd.cs, e1 = rd.w.cigar_offsets[c + 1] - rd.cs;
+        const u32 op = op_code(b.cigars[c]);
+        if (op == OP_M) {
+            for (u32 i = e0; i < e1; i++) {
+                cur = rd.readc(i);
+                const u8 rbp = rd.sym(cur);
+                const u8 fbp = contig_at(*g, u64(rd.astart) + rd.refc(i));
+                if (fbp != rbp) {
+                    bf[cur] |= BF_SNP;
+                    if (cur >= w.x && cur <= w.y) nerr++;
+                }
+            }
+        } else if (op == OP_I) {
+            cur = u16(rd.w.ev_rc[rd.cs + e0] & 0xFFFF);
+            if (cur >= w.x && cur <= w.y) {
+                const int off = neg ? int(cur) + int(op_len(b.cigars[c])) : int(cur) - 1;
+                if (off >= 0 && off <= int(w.y)) {
+                    bf[off] |= BF_INS;
+                    nerr++;
+                }
+            }
+        } else if (op == OP_D) {
+            const u16 cref = u16(rd.w.ev_rc[rd.cs + e0] >> 16);
+            if (cref >= rw.x && cref <= rw.y) {
+                if (!neg) {
+                    bf[cur] |= BF_DEL;
+                    nerr++;
+                } else {
+                    const u16 off = u16(cur + 1);
+                    if (off < rd.rlen) {
+                        bf[off] |= BF_DEL;
+                        nerr++;
+                    }
+                }
+            }
+        }
+    }
+    return nerr;
+}
+
+// lower_bound / upper_bound (device/primitives/algorithms.h:39-100)
+__device__ u32 ref_lower_bound(u32 x, const u32 *a, u32 n) {
+    if (n == 0) return 0;
+    if (x < a[0]) return 0;
+    if (a[n - 1] < x) return n;
+    u32 base = 0, count = n;
+    while (count > 0) {
+        const u32 c2 = count / 2, mid = base + c2;
+        if (a[mid] < x) { base = mid + 1; count -= c2 + 1; } else { count = c2; }
+    }
+    return base;
+}
+__device__ u32 ref_upper_bound(u32 x, const u32 *a, u32 n) {
+    u32 base = 0, count = n;
+    while (count > 0) {
+        const u32 step = count / 2, it = base + step;
+        if (!(x < a[it])) { base = it + 1; count -= step + 1; } else { count = step; }
+    }
+    return base;
+}
+
+// compute_vcf_ranges + filter_bps (device/snp_filter.cu:162-395)
+__device__ void filter_known_sites(const Read &rd, us2 w, us2 rw, u8 *bf) {
+    const u32 ch = rd.b.chromosome[rd.r];
+    if (ch >= rd.ref.num_site_contigs) return;
+    const DevSites db = rd.ref.sites[ch];
+    const u32 wx = rd.astart + u32(rw.x), wy = rd.astart + u32(rw.y);
+    const u32 vx = ref_lower_bound(wx, db.maxend, db.n);
+    if (vx >= db.n) return;
+    u32 vy = ref_upper_bound(wy, db.start, db.n);
+    if (vy <= vx) return;
+    if (vy >= db.n) vy = db.n - 1;
+    const u32 n = rd.n;
+    for (u32 feature = vx; feature <= vy; feature++) {
+        const int fstart = int(db.start[feature] - rd.astart);
+        const int fend = int(db.stop[feature] - rd.astart);
+        u32 ev;
+        u16 ref_coord = U16_NONE;
+        for (ev = 0; ev < n; ev++) {
+            ref_coord = rd.refc(ev);
+            if (ref_coord != U16_NONE && int(ref_coord) >= fstart) break;
+        }
+        if (ev == n) continue;
+        int left = int(ref_coord) - fstart;
+        u32 evs = ev;
+        if (left > 0) {
+            while (left && evs > 0) {
+                const u8 t = rd.ty[evs];
+                if (t == EV_S) break;
+                if (t == EV_M || t == EV_D) left--;
+                evs--;
+            }
+            while (evs > 0 && rd.ty[evs - 1] == EV_I) evs--;
+            while (evs < n && rd.readc(evs) == U16_NONE) evs++;
+        } else {
+            if (rd.refc(evs) <= rw.y) {
+                while (evs > 0 && rd.ty[evs] == EV_D) evs--;
+            }
+        }
+        int right = fend - int(ref_coord);
+        while (right > 0 && ev + 1 < n) {
+            ev++;
+            const u8 t = rd.ty[ev];
+            if (t == EV_S) break;
+            if (t == EV_M || t == EV_D) right--;
+        }
+        while (ev > 0 && rd.readc(ev) == U16_NONE) ev--;
+        if (ev < evs) continue;
+        u32 a = rd.readc(evs), z = rd.readc(ev);
+        if ((a < w.x && z < w.x) || (a > w.y && z > w.y)) continue;
+        a = tmin<u32>(tmax<u32>(a, w.x), w.y);
+        z = tmin<u32>(tmax<u32>(z, w.x), w.y);
+        for (u32 d = a; d <= z; d++) bf[d] &= u8(~BF_ACTIVE);
+    }
+}
+
+// compute_hmm_windows (device/baq.cu:89-187)
+__device__ bool hmm_window(const Read &rd, const DevContig *g, u16 nerr, us2 w, us2 ni, us2 rw, ss2 &hw, u16 &bw) {
+    const bool needs = nerr != 0;
+    const int offset = MIN_BAND_WIDTH / 2;
+    const bool left_clip = w.x != 0;
+    const bool right_clip = w.y != u16(rd.rlen - 1);
+    const i16 li = i16(left_clip ? 0 : int(ni.x) - int(w.x));
+    const i16 ri = i16(right_clip ? 0 : int(w.y) - int(ni.y));
+    hw.x = i16(int(rw.x) - li - offset);
+    hw.y = i16(int(rw.y) + ri + offset);
+    const u64 csize = g ? g->size : 0;
+    int shift = 0;
+    if (hw.x < 0 && rd.astart < baq_abs(hw.x)) shift = -1;
+    if (needs && u32(rd.astart + u32(int(hw.y)) + u32(shift)) >= u32(csize)) {
+        hw.x = -1;
+        hw.y = -1;
+        return false;
+    }
+    const int refLen = hw.y - hw.x + 1;
+    const int qLen = w.y - w.x + 1;
+    u16 band = u16(refLen > qLen ? refLen : qLen);
+    const u32 d = baq_abs(refLen - qLen);
+    if (u32(MIN_BAND_WIDTH) < d) band = u16(d + 3);
+    if (band > MIN_BAND_WIDTH) band = MIN_BAND_WIDTH;
+    if (band < d) band = u16(d);
+    bw = band;
+    return true;
+}
+
+__global__ void __launch_bounds__(128) k_prep(DevBatch b, DevRef ref, BatchWork w) {
+    const u32 r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= b.R) return;
+    u8 status = RS_FILTERED;
+    u32 filtered = 0;
+    const u32 qs = b.qual_start[r];
+    const u32 rlen = b.read_len[r];
+    u8 *bf = w.bflags + qs;
+
+    // filter_invalid_reads -> alignment windows -> filter_malformed_reads (device/pipeline.cu:66-80)
+    bool pass = passes_invalid_filters(b, r);
+    if (pass) {
+        u32 wx, wy, covered;
+        bool bad_op;
+        alignment_window(b, r, wx, wy, covered, bad_op);
+        // filter_if_read_malformed (device/read_filters.cu:77-154); the uint16 contig id never equals
+        // uint32(-1), so those checks are inert. Unknown contigs fail the contig-end check; reads whose
+        // CIGAR does not cover read_len bases or holds an op code above X are rejected (undefined in the
+        // reference).
+        const u32 ch = b.chromosome[r];
+        const DevContig *g = contig_of(ref, ch);
+        if (!(b.flags[r] & F_UNMAP)) {
+            if (b.astart[r] == U32_NONE) pass = false;
+            else if (wy <= wx) pass = false;
+            else if (wx >= (g ? g->size : 0)) pass = false;
+            else if (b.cigar_len[r] == 0) pass = false;
+        }
+        if (b.rg[r] == U32_NONE) pass = false;
+        if (b.qual_len[r] != rlen) pass = false;
+        if (rlen == 0) pass = false;
+        if (covered != rlen || bad_op) pass = false;
+    }
+    if (!pass) {
+        filtered = 1;
+        w.status[r] = RS_FILTERED;
+        atomicAdd(&w.counters[5], filtered);
+        return;
+    }
+
+    Read rd(b, ref, w, r);
+    const DevContig *g = contig_of(ref, b.chromosome[r]);
+    expand_read(rd);
+
+    // start_batch: every base active (device/firepony_context.cu:52-59); error bits cleared
+    for (u32 i = 0; i < rlen; i++) bf[i] = BF_ACTIVE;
+
+    us2 wcl = {0, u16(rlen - 1)};  // read_window_init (device/cigar.cu:97-109)
+    remove_adapters(rd, wcl);
+    remove_soft_clips(rd, wcl);
+    const us2 ni = no_insertions_window(rd, wcl);
+    const us2 rw = reference_window(rd, ni);
+    const u16 nerr = error_vectors(rd, g, wcl, rw, bf);
+
+    // filter_bases (device/read_filters.cu:375-439)
+    for (u32 i = 0; i < rlen; i++) {
+        const u8 bp = rd.sym(i);
+        const bool regular = bp == IUPAC_A || bp == IUPAC_C || bp == IUPAC_G || bp == IUPAC_T;
+        if (!regular || b.quals[qs + i] < 6) bf[i] &= u8(~BF_ACTIVE);
+    }
+    filter_known_sites(rd, wcl, rw, bf);
+
+    ss2 hw;
+    u16 bw = 0;
+    const bool hmm_ok = hmm_window(rd, g, nerr, wcl, ni, rw, hw, bw);
+    status = hmm_ok ? RS_ACTIVE : RS_REMOVED;
+    if (!hmm_ok) {
+        // the read's events lose their read coordinates (device/baq.cu:136-158): it contributes nothing
+        for (u32 e = 0; e < rd.n; e++) rd.rc[e] = u32(U16_NONE) | (rd.rc[e] & 0xFFFF0000u);
+    }
+
+    u16 *win = w.win + size_t(r) * 8;
+    win[0] = wcl.x; win[1] = wcl.y; win[2] = ni.x; win[3] = ni.y; win[4] = rw.x; win[5] = rw.y;
+    w.hmm[size_t(r) * 2 + 0] = hw.x;
+    w.hmm[size_t(r) * 2 + 1] = hw.y;
+    w.bw[r] = bw;
+    w.nerr[r] = nerr;
+    w.status[r] = status;
+
+    if (status == RS_ACTIVE) {
+        if (nerr != 0) {
+            // BAQ work list by band class: 0 -> bw <= 7, 1 -> bw <= 15, 2 -> wider
+            const u32 cls = bw <= 7 ? 0 : (bw <= 15 ? 1 : 2);
+            const u32 slot = atomicAdd(&w.counters[cls], 1u);
+            w.baq_list[size_t(cls) * b.R + slot] = r;
+            atomicAdd(&w.counters[6], 1u);
+            atomicMax(&w.counters[7], u32(wcl.y - wcl.x + 1));
+            atomicMax(&w.counters[12 + cls], u32(bw));
+        } else {
+            // read_flat_baq (device/baq.cu:842-868)
+            for (u32 i = wcl.x; i <= wcl.y; i++) w.tag[qs + i] = NO_BAQ_UNCERTAINTY;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// cap_baq_qualities + recode_baq_qualities (device/baq.cu:870-1081) for one BAQ read. In FP32 mode
+// (exact == 0) the HMM outputs can be undecided (baq_amb); if the cap depends on an undecided value the
+// read goes to the escalation list and nothing is written.
+__global__ void __launch_bounds__(128) k_cap(DevBatch b, BatchWork w, const u32 *list, const u32 *count, int exact) {
+    const u32 idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= *count) return;
+    const u32 r = list[idx];
+    const u32 cs = w.cigar_offsets[b.cigar_start[r]];
+    const u32 ce = w.cigar_offsets[b.cigar_start[r] + b.cigar_len[r]];
+    const u32 n = ce - cs;
+    const u32 *rc = w.ev_rc + cs;
+    const u8 *ty = w.ev_type + cs;
+    const u16 *win = w.win + size_t(r) * 8;
+    const us2 wcl = {win[0], win[1]}, rw = {win[4], win[5]};
+    const ss2 hw = {w.hmm[size_t(r) * 2], w.hmm[size_t(r) * 2 + 1]};
+    const u32 qs = b.qual_start[r];
+    const u32 astart = b.astart[r];
+
+    u32 baq_start = 0;
+    for (u32 i = 0; i < n; i++) {
+        const u16 rb = u16(rc[i] & 0xFFFF);
+        if (rb != U16_NONE && rb >= wcl.x) { baq_start = i; break; }
+    }
+    i16 reference_shift = 0, read_shift = 0;
+    if (hw.x < 0 && astart < baq_abs(hw.x)) {
+        reference_shift = i16(baq_abs(hw.x));
+        read_shift = i16(astart);
+    }
+    const i16 refOffset = i16(int(hw.x) - int(rw.x) + int(reference_shift));
+
+    // pass 1: cap_baq<false> — count read bases; pass 2: cap_baq<true> (or decide escalation)
+    u32 readI = 0;
+    for (u32 i = baq_start; i < n; i++) {
+        const u16 rb = u16(rc[i] & 0xFFFF);
+        if (rb != U16_NONE) {
+            if (rb < wcl.x) continue;
+            if (rb > wcl.y) break;
+        }
+        const u8 t = ty[i];
+        if (t == EV_I || t == EV_M) readI++;
+    }
+    const bool need_update = readI == u32(wcl.y - wcl.x + 1);
+
+    if (need_update) {
+        if (!exact) {
+            // does any capped value depend on an undecided HMM output?
+            u32 refI = 0, numD = 0;
+            readI = 0;
+            bool escalate = false;
+            for (u32 i = baq_start; i < n && !escalate; i++) {
+                const u16 rb = u16(rc[i] & 0xFFFF);
+                if (rb != U16_NONE) {
+                    if (rb < wcl.x) continue;
+                    if (rb > wcl.y) break;
+                }
+                switch (ty[i]) {
+                case EV_S: refI++; break;
+                case EV_I: readI++; break;
+                case EV_D: refI++; numD++; break;
+                case EV_M: {
+                    const u8 amb = w.baq_amb[qs + rb];
+                    if (amb & 2) {
+                        escalate = true;
+                    } else {
+                        const u32 expectedPos = refI - u32(int(refOffset)) + (i - numD - baq_start - readI) + u32(int(read_shift));
+                        const u32 state = w.baq_state[qs + rb];
+                        const bool decided_min = ((state & 3) != 0) || ((state >> 2) != expectedPos);
+                        if (!decided_min && (amb & 1)) escalate = true;
+                    }
+                    readI++;
+                    refI++;
+                    break;
+                }
+                }
+            }
+            if (escalate) {
+                const u32 slot = atomicAdd(&w.counters[4], 1u);
+                w.esc_list[slot] = r;
+                return;
+            }
+        }
+        u32 refI = 0, numD = 0;
+        readI = 0;
+        for (u32 i = baq_start; i < n; i++) {
+            const u16 rb = u16(rc[i] & 0xFFFF);
+            if (rb != U16_NONE) {
+                if (rb < wcl.x) continue;
+                if (rb > wcl.y) break;
+            }
+            switch (ty[i]) {
+            case EV_S: refI++; break;
+            case EV_I: w.tag[qs + rb] = b.quals[qs + rb]; readI++; break;
+            case EV_D: refI++; numD++; break;
+            case EV_M: {
+                const u32 expectedPos = refI - u32(int(refOffset)) + (i - numD - baq_start - readI) + u32(int(read_shift));
+                const u8 oq = b.quals[qs + rb];
+                const u8 bq = w.baq_q[qs + rb];
+                const u32 state = w.baq_state[qs + rb];
+                const bool isIndel = (state & 3) != 0;
+                const u32 pos = state >> 2;
+                w.tag[qs + rb] = (isIndel || pos != expectedPos) ? u8(MIN_BASE_QUAL) : (bq < oq ? bq : oq);
+                readI++;
+                refI++;
+                break;
+            }
+            }
+        }
+    } else {
+        for (u32 i = wcl.x; i <= wcl.y; i++) w.tag[qs + i] = b.quals[qs + i];
+    }
+    // recode_baq_qualities (device/baq.cu:1058-1081)
+    const u32 ql = b.qual_len[r];
+    for (u32 i = 0; i < ql; i++) {
+        const u8 v = w.tag[qs + i];
+        if (v == 0xFF) continue;
+        w.tag[qs + i] = u8(u8(b.quals[qs + i] + 64) - v);
+    }
+}
+
+}  // namespace
+
+void launch_validate(const DevBatch &b, u32 n_rg, u32 *err, cudaStream_t s) {
+    if (!b.R) return;
+    k_validate<<<(b.R + 255) / 256, 256, 0, s>>>(b, n_rg, err);
+    g_kernel_launches++;
+}
+
+void launch_op_lengths(const DevBatch &b, u32 *out, cudaStream_t s) {
+    if (!b.num_cigar_ops) return;
+    k_op_lengths<<<(b.num_cigar_ops + 255) / 256, 256, 0, s>>>(b, out);
+    g_kernel_launches++;
+}
+
+void launch_prep(const DevBatch &b, const DevRef &ref, const BatchWork &w, cudaStream_t s) {
+    if (!b.R) return;
+    k_prep<<<(b.R + 127) / 128, 128, 0, s>>>(b, ref, w);
+    g_kernel_launches++;
+}
+
+void launch_cap(const DevBatch &b, const BatchWork &w, const u32 *list, const u32 *count, int exact, cudaStream_t s,
+                u32 max_reads) {
+    if (!max_reads) return;
+    k_cap<<<(max_reads + 127) / 128, 128, 0, s>>>(b, w, list, count, exact);
+    g_kernel_launches++;
+}
+
+}  // namespace fpg

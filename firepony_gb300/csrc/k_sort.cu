@@ -1,0 +1,255 @@
+// K4: exclusive scan, stable LSD radix sort of packed 64-bit covariate entries (dense key in the high 32
+// bits, float mismatch bits in the low 32), and the ordered segmented fold into the resident mismatch
+// table. Stable sorting keeps each key's entries in stream order, so folding a segment left to right from
+// the running total reproduces the reference's append + stable sort + reduce_by_key of every batch
+// (device/covariates.cu:172-201, device/covariate_table.cu:43-107) as one sequential float sum per key.
+#include "kernels.h"
+
+namespace fpg {
+
+namespace {
+
+constexpr u32 FULL = 0xffffffffu;
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_ITEMS = 4;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+// block-wide exclusive scan of one value per thread; returns the block total in *total
+__device__ u32 block_exclusive_scan(u32 v, u32 *total) {
+    __shared__ u32 warp_sums[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    u32 x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const u32 y = __shfl_up_sync(FULL, x, d);
+        if (lane >= d) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+        u32 s = lane < nw ? warp_sums[lane] : 0;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const u32 y = __shfl_up_sync(FULL, s, d);
+            if (lane >= d) s += y;
+        }
+        if (lane < nw) warp_sums[lane] = s;
+    }
+    __syncthreads();
+    const u32 warp_prefix = warp ? warp_sums[warp - 1] : 0;
+    *total = warp_sums[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return warp_prefix + x - v;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const u32 *in, u64 n, u32 *sums) {
+    const u64 base = u64(blockIdx.x) * SCAN_TILE + u64(threadIdx.x) * SCAN_ITEMS;
+    u32 s = 0;
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; j++)
+        if (base + j < n) s += in[base + j];
+    u32 total;
+    block_exclusive_scan(s, &total);
+    if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const u32 *in, u64 n, const u32 *offsets, u32 *out) {
+    const u64 base = u64(blockIdx.x) * SCAN_TILE + u64(threadIdx.x) * SCAN_ITEMS;
+    u32 v[SCAN_ITEMS];
+    u32 s = 0;
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; j++) {
+        v[j] = base + j < n ? in[base + j] : 0;
+        s += v[j];
+    }
+    u32 total;
+    u32 p = block_exclusive_scan(s, &total) + (offsets ? offsets[blockIdx.x] : 0);
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; j++) {
+        if (base + j < n) out[base + j] = p;
+        p += v[j];
+    }
+}
+
+__global__ void k_scan_total(const u32 *in, u64 n, u32 *out) {
+    // out[n] = out[n-1] + in[n-1]
+    if (n) out[n] = out[n - 1] + in[n - 1];
+    else out[0] = 0;
+}
+
+void scan_rec(const u32 *in, u32 *out, u64 n, u32 *tmp, cudaStream_t s) {
+    const u64 blocks = (n + SCAN_TILE - 1) / SCAN_TILE;
+    if (blocks <= 1) {
+        k_scan_apply<<<1, SCAN_THREADS, 0, s>>>(in, n, nullptr, out);
+        g_kernel_launches++;
+    } else {
+        u32 *sums = tmp;
+        u32 *sums_scan = tmp + blocks + 1;
+        k_scan_reduce<<<u32(blocks), SCAN_THREADS, 0, s>>>(in, n, sums);
+        scan_rec(sums, sums_scan, blocks, sums_scan + blocks + 1, s);
+        k_scan_apply<<<u32(blocks), SCAN_THREADS, 0, s>>>(in, n, sums_scan, out);
+        g_kernel_launches += 2;
+    }
+    k_scan_total<<<1, 1, 0, s>>>(in, n, out);
+    g_kernel_launches++;
+}
+
+// ---- radix sort ----
+constexpr int RS_THREADS = 256;
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int RS_ROUNDS = 8;
+constexpr int RS_TILE = RS_THREADS * RS_ROUNDS;
+
+__device__ __forceinline__ u32 digit_of(u64 v, int shift) { return u32(v >> (32 + shift)) & 0xFFu; }
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const u64 *in, u64 n, int shift, u32 *hist, u32 nblocks) {
+    __shared__ u32 h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const u64 base = u64(blockIdx.x) * RS_TILE;
+    for (int rnd = 0; rnd < RS_ROUNDS; rnd++) {
+        const u64 i = base + u64(rnd) * RS_THREADS + threadIdx.x;
+        if (i < n) atomicAdd(&h[digit_of(in[i], shift)], 1u);
+    }
+    __syncthreads();
+    hist[u64(threadIdx.x) * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const u64 *in, u64 n, int shift, const u32 *offs,
+                                                           u32 nblocks, u64 *out) {
+    __shared__ u32 running[256];
+    __shared__ u32 wc[RS_WARPS][256];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    running[threadIdx.x] = offs[u64(threadIdx.x) * nblocks + blockIdx.x];
+    const u64 base = u64(blockIdx.x) * RS_TILE;
+    const u32 lt = (1u << lane) - 1;
+    for (int rnd = 0; rnd < RS_ROUNDS; rnd++) {
+        for (int j = threadIdx.x; j < RS_WARPS * 256; j += RS_THREADS) (&wc[0][0])[j] = 0;
+        __syncthreads();
+        const u64 i = base + u64(rnd) * RS_THREADS + threadIdx.x;
+        const bool valid = i < n;
+        const u64 v = valid ? in[i] : 0;
+        const u32 d = valid ? digit_of(v, shift) : 256u;
+        const u32 peers = __match_any_sync(FULL, d);
+        const u32 rank = __popc(peers & lt);
+        if (valid && rank == 0) wc[warp][d] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            u32 pre = 0;
+            for (int w2 = 0; w2 < warp; w2++) pre += wc[w2][d];
+            out[running[d] + pre + rank] = v;
+        }
+        __syncthreads();
+        {
+            u32 tot = 0;
+            for (int w2 = 0; w2 < RS_WARPS; w2++) tot += wc[w2][threadIdx.x];
+            running[threadIdx.x] += tot;
+        }
+        __syncthreads();
+    }
+}
+
+// ---- ordered fold ----
+__global__ void k_heads(const u64 *s, u64 n, u32 *flag) {
+    const u64 i = u64(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    flag[i] = (i == 0 || (s[i] >> 32) != (s[i - 1] >> 32)) ? 1u : 0u;
+}
+
+__global__ void k_head_list(const u32 *flag, const u32 *pos, u64 n, u32 *heads) {
+    const u64 i = u64(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (flag[i]) heads[pos[i]] = u32(i);
+}
+
+// one warp per segment (grid-stride over segments): lanes load 32 entries at a time (coalesced) and the
+// sum runs through them in order
+__global__ void k_fold(const u64 *s, u64 n, const u32 *heads, const u32 *num_heads, float *mism) {
+    const u32 nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const u32 nh = *num_heads;
+    for (u32 h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; h < nh; h += nwarps) {
+        const u64 start = heads[h];
+        const u64 end = (h + 1 < nh) ? heads[h + 1] : n;
+        const u32 key = u32(s[start] >> 32);
+        float acc = mism[key];
+        for (u64 c = start; c < end; c += 32) {
+            const u64 i = c + lane;
+            const float v = i < end ? __uint_as_float(u32(s[i])) : 0.0f;
+            const int cnt = int(end - c < 32 ? end - c : 32);
+            for (int j = 0; j < cnt; j++) {
+                const float x = __shfl_sync(FULL, v, j);
+                acc = __fadd_rn(acc, x);
+            }
+        }
+        if (lane == 0) mism[key] = acc;
+    }
+}
+
+}  // namespace
+
+size_t scan_tmp_bytes(u64 n) {
+    // sums and scanned sums for every level
+    u64 total = 0;
+    u64 m = n;
+    while (m > u64(SCAN_TILE)) {
+        m = (m + SCAN_TILE - 1) / SCAN_TILE;
+        total += 2 * (m + 1);
+    }
+    return size_t(total + 64) * sizeof(u32);
+}
+
+void launch_exclusive_scan(const u32 *in, u32 *out, u64 n, void *tmp, cudaStream_t s) {
+    scan_rec(in, out, n, reinterpret_cast<u32 *>(tmp), s);
+}
+
+size_t radix_tmp_bytes(u64 n) {
+    const u64 nblocks = (n + RS_TILE - 1) / RS_TILE + 1;
+    const u64 hist = nblocks * 256;
+    return size_t(2 * (hist + 1)) * sizeof(u32) + scan_tmp_bytes(hist) + 256;
+}
+
+size_t fold_tmp_bytes(u64 n) { return size_t(3 * (n + 1)) * sizeof(u32) + scan_tmp_bytes(n) + 256; }
+
+void launch_radix_sort(u64 *keys, u64 *alt, u64 n, int key_bits, void *tmp, size_t tmp_bytes, u64 **result,
+                       cudaStream_t s) {
+    (void)tmp_bytes;
+    u64 *src = keys, *dst = alt;
+    if (n > 1) {
+        const u32 nblocks = u32((n + RS_TILE - 1) / RS_TILE);
+        const u64 hist_n = u64(nblocks) * 256;
+        u32 *hist = reinterpret_cast<u32 *>(tmp);
+        u32 *offs = hist + hist_n + 1;
+        void *stmp = offs + hist_n + 1;
+        for (int shift = 0; shift < key_bits; shift += 8) {
+            k_rs_hist<<<nblocks, RS_THREADS, 0, s>>>(src, n, shift, hist, nblocks);
+            scan_rec(hist, offs, hist_n, reinterpret_cast<u32 *>(stmp), s);
+            k_rs_scatter<<<nblocks, RS_THREADS, 0, s>>>(src, n, shift, offs, nblocks, dst);
+            g_kernel_launches += 2;
+            u64 *t = src;
+            src = dst;
+            dst = t;
+        }
+    }
+    *result = src;
+}
+
+void launch_fold(const u64 *sorted, u64 n, float *mism, void *tmp, cudaStream_t s) {
+    if (!n) return;
+    u32 *flag = reinterpret_cast<u32 *>(tmp);
+    u32 *pos = flag + n + 1;
+    u32 *heads = pos + n + 1;
+    void *stmp = heads + n + 1;
+    const u32 blocks = u32((n + 255) / 256);
+    k_heads<<<blocks, 256, 0, s>>>(sorted, n, flag);
+    scan_rec(flag, pos, n, reinterpret_cast<u32 *>(stmp), s);
+    k_head_list<<<blocks, 256, 0, s>>>(flag, pos, n, heads);
+    // number of segments = pos[n]; a fixed grid of warps strides over them
+    u64 fold_blocks = (n * 32 + 255) / 256;
+    if (fold_blocks > 152 * 16) fold_blocks = 152 * 16;
+    k_fold<<<u32(fold_blocks), 256, 0, s>>>(sorted, n, heads, pos + n, mism);
+    g_kernel_launches += 3;
+}
+
+}  // namespace fpg

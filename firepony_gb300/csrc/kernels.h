@@ -1,0 +1,112 @@
+// Host-side launch interface of the engine's kernels (one function per kernel or kernel group).
+#pragma once
+
+#include "common.cuh"
+
+namespace fpg {
+
+// Per-batch device work arrays (owned by the engine, sized per batch).
+struct BatchWork {
+    // events (expanded CIGAR): one entry per CIGAR op length unit
+    u32 *cigar_offsets;      // num_cigar_ops + 1 (exclusive scan of op lengths)
+    u32 *ev_rc;              // read coordinate | reference coordinate << 16
+    u8 *ev_type;
+    u64 num_events;
+    // per read
+    u8 *status;
+    u16 *win;                // 8 x u16: clipped, no-ins, reference, high-quality windows
+    i16 *hmm;                // 2 x i16 HMM reference window
+    u16 *bw;
+    u16 *nerr;
+    // per base (quality index space)
+    u8 *bflags;
+    u8 *tag;                 // BQ tag after recode (0xFF where none)
+    u8 *baq_q;               // HMM MAP quality
+    u32 *baq_state;          // HMM MAP state
+    u8 *baq_amb;             // FP32 HMM: bit0 quality undecided, bit1 state undecided
+    float *frac;             // 3 x float per base (snp, ins, del fractional errors as stored in the table)
+    // work lists
+    u32 *baq_list;           // reads that need BAQ, by band class
+    u32 *counters;           // [0..3] list sizes per class, [4] escalated count, [5] filtered, [6] baq reads
+    u32 *esc_list;
+    // covariate entries
+    u32 *entry_count;        // per read + 1
+    u32 *entry_offset;       // per read + 1 (exclusive scan)
+    u64 *entries;
+    u64 *entries_alt;
+    u64 entry_capacity;
+    // scratch
+    void *scan_tmp;
+    size_t scan_tmp_bytes;
+    u32 *err;
+};
+
+struct Tables {
+    KeySpace ks;
+    unsigned long long *obs;  // per dense key
+    float *mism;              // per dense key
+};
+
+// HMM constants computed on the host with the platform libm (exactly the reference's host values)
+struct HmmConst {
+    double qual2prob[256];
+    double gap_open;
+};
+
+// k_prep.cu
+void launch_validate(const DevBatch &b, u32 n_rg, u32 *err, cudaStream_t s);
+void launch_op_lengths(const DevBatch &b, u32 *out, cudaStream_t s);
+void launch_prep(const DevBatch &b, const DevRef &ref, const BatchWork &w, cudaStream_t s);
+void launch_cap(const DevBatch &b, const BatchWork &w, const u32 *list, const u32 *count, int exact,
+                cudaStream_t s, u32 max_reads);
+
+// k_baq64.cu
+void baq64_set_constants(const HmmConst &c);
+void launch_baq64(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
+                  u32 max_reads, double *scratch, u64 scratch_doubles, u32 max_qlen, u32 max_bw, cudaStream_t s);
+u64 baq64_scratch_doubles(u32 threads, u32 max_qlen, u32 max_bw);
+u32 baq64_threads();
+
+// k_baq32.cu
+void baq32_set_constants(const HmmConst &c);
+void launch_baq32(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
+                  u32 max_reads, int group_lanes, float *scratch, u32 max_qlen, cudaStream_t s);
+u64 baq32_scratch_floats(int group_lanes, u32 max_qlen);
+
+// k_covariates.cu
+void launch_cov_count(const DevBatch &b, const BatchWork &w, const Tables &t, cudaStream_t s);
+void launch_cov_emit(const DevBatch &b, const BatchWork &w, const Tables &t, cudaStream_t s);
+
+// k_sort.cu
+size_t scan_tmp_bytes(u64 n);
+void launch_exclusive_scan(const u32 *in, u32 *out, u64 n, void *tmp, cudaStream_t s);  // out has n+1 entries
+void launch_radix_sort(u64 *keys, u64 *alt, u64 n, int key_bits, void *tmp, size_t tmp_bytes, u64 **result,
+                       cudaStream_t s);
+size_t radix_tmp_bytes(u64 n);
+size_t fold_tmp_bytes(u64 n);
+void launch_fold(const u64 *sorted, u64 n, float *mism, void *tmp, cudaStream_t s);
+
+// k_post.cu
+struct PostTables {
+    // compacted observation rows of the three tables, in ascending dense key (== ascending reference key)
+    u32 *dense;                  // dense key per row
+    u32 num_rows;
+};
+void launch_mark_nonzero(const Tables &t, u32 *flags, cudaStream_t s);
+void launch_gather_rows(const Tables &t, const u32 *flags, const u32 *pos, u32 *rows_dense, cudaStream_t s);
+// empirical quality per row (device/empirical_quality.cu:35-198) with host libm constants
+struct EmpConst {
+    double prior[41];            // log10(gaussian(difference)), difference 0..40
+    double log10p[61];           // bin / -10.0
+    double log10_one_minus_p[61];
+};
+void post_set_constants(const EmpConst &c, const double *qual2err);
+void launch_rows(const Tables &t, const u32 *rows, u32 n, u32 *key, u64 *obs, double *mism, double *exp_,
+                 double *est, cudaStream_t s);
+void launch_rg_fold(const Tables &t, u64 *rg_obs, double *rg_mism, double *rg_exp, cudaStream_t s);
+void launch_empirical(u32 n, const u64 *obs, const double *mism, const double *est, const double *binom_coef,
+                      int need_rounding, double *emp_out, cudaStream_t s);
+
+extern unsigned long long g_kernel_launches;
+
+}  // namespace fpg

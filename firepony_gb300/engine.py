@@ -1,0 +1,222 @@
+"""Python binding of the C ABI in include/firepony_gb300.h (ctypes over the in-tree libfpengine.so).
+
+The compute path is the CUDA engine only: if the native library cannot be loaded, or no GPU is present, the
+calls raise. There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from .abi import (FP_OK, STATUS_NAMES, FpBatchView, FpOptions, FpStats, FpTableView, FP_BAQ_FP32, FP_BAQ_FP64,
+                  table_to_numpy)
+
+_BUILD = Path(__file__).resolve().parent / "_build"
+_lib = None
+
+EXPORTED = [
+    "fp_engine_create", "fp_engine_destroy", "fp_last_error", "fp_engine_set_contig", "fp_engine_set_known_sites",
+    "fp_engine_submit_batch", "fp_engine_finalize", "fp_engine_get_table", "fp_engine_write_report",
+    "fp_engine_reset", "fp_engine_get_stats", "fp_engine_debug_last_batch", "fp_report_write", "fp_host_alloc",
+    "fp_host_free", "fp_engine_submit_batch_device", "fp_engine_cuda_stream",
+]
+
+
+class EngineError(RuntimeError):
+    pass
+
+
+def library_path() -> Path:
+    return _BUILD / "libfpengine.so"
+
+
+def lib():
+    """Loads libfpengine.so (building it first if it is missing)."""
+    global _lib
+    if _lib is None:
+        p = library_path()
+        if not p.exists():
+            from .build import build_engine
+            build_engine()
+        L = C.CDLL(str(p))
+        L.fp_engine_create.argtypes = [C.POINTER(FpOptions), C.POINTER(C.c_void_p)]
+        L.fp_engine_destroy.argtypes = [C.c_void_p]
+        L.fp_last_error.restype = C.c_char_p
+        L.fp_last_error.argtypes = [C.c_void_p]
+        L.fp_engine_set_contig.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint64]
+        L.fp_engine_set_known_sites.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32]
+        L.fp_engine_submit_batch.argtypes = [C.c_void_p, C.POINTER(FpBatchView)]
+        L.fp_engine_finalize.argtypes = [C.c_void_p]
+        L.fp_engine_get_table.argtypes = [C.c_void_p, C.c_int32, C.POINTER(FpTableView)]
+        L.fp_engine_write_report.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_char_p), C.c_uint32, C.c_int,
+                                             C.c_int, C.c_int, C.c_int]
+        L.fp_engine_reset.argtypes = [C.c_void_p]
+        L.fp_engine_get_stats.argtypes = [C.c_void_p, C.POINTER(FpStats)]
+        L.fp_engine_debug_last_batch.argtypes = [C.c_void_p] + [C.c_void_p] * 6
+        L.fp_report_write.argtypes = [C.c_char_p, C.POINTER(FpTableView), C.POINTER(C.c_char_p), C.c_uint32, C.c_int,
+                                      C.c_int, C.c_int, C.c_int]
+        L.fp_engine_submit_batch_device.argtypes = [C.c_void_p, C.POINTER(FpBatchView)]
+        L.fp_engine_cuda_stream.restype = C.c_void_p
+        L.fp_engine_cuda_stream.argtypes = [C.c_void_p]
+        L.fp_host_alloc.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
+        L.fp_host_free.argtypes = [C.c_void_p]
+        _lib = L
+    return _lib
+
+
+def _names(rg_names):
+    arr = (C.c_char_p * max(1, len(rg_names)))(*[n.encode() for n in rg_names])
+    return arr
+
+
+def write_report(path, tables: dict, rg_names, disable_rounding=False, version=(1, 1, 1)):
+    """Writes a GATKReport from numpy tables (the layout returned by Engine.finalize / Oracle.finalize)."""
+    keep = []
+    views = (FpTableView * 4)()
+    for t in range(4):
+        d = tables[t]
+        arrs = [np.ascontiguousarray(d[k]) for k in ("keys", "observations", "mismatches", "expected_errors",
+                                                     "estimated_quality", "empirical_quality")]
+        keep.append(arrs)
+        v = views[t]
+        v.num_rows = len(arrs[0])
+        v.keys = arrs[0].ctypes.data_as(C.POINTER(C.c_uint32))
+        v.observations = arrs[1].ctypes.data_as(C.POINTER(C.c_uint64))
+        v.mismatches = arrs[2].ctypes.data_as(C.POINTER(C.c_double))
+        v.expected_errors = arrs[3].ctypes.data_as(C.POINTER(C.c_double))
+        v.estimated_quality = arrs[4].ctypes.data_as(C.POINTER(C.c_double))
+        v.empirical_quality = arrs[5].ctypes.data_as(C.POINTER(C.c_double))
+    rc = lib().fp_report_write(str(path).encode(), views, _names(rg_names), len(rg_names), int(disable_rounding),
+                               *version)
+    if rc != FP_OK:
+        raise EngineError(f"fp_report_write: {STATUS_NAMES.get(rc, rc)}")
+
+
+class Engine:
+    """One GB300 BQSR engine (fp_engine handle)."""
+
+    def __init__(self, num_read_groups: int = 1, baq_mode: str = "fp32", device: int = 0):
+        o = FpOptions()
+        o.device = device
+        o.baq_mode = FP_BAQ_FP64 if baq_mode == "fp64" else FP_BAQ_FP32
+        o.num_read_groups = num_read_groups
+        h = C.c_void_p()
+        rc = lib().fp_engine_create(C.byref(o), C.byref(h))
+        if rc != FP_OK:
+            raise EngineError(f"fp_engine_create failed: {STATUS_NAMES.get(rc, rc)}")
+        self.h = h
+        self.num_read_groups = num_read_groups
+
+    def _check(self, rc, what):
+        if rc != FP_OK:
+            msg = lib().fp_last_error(self.h)
+            raise EngineError(f"{what}: {STATUS_NAMES.get(rc, rc)}: {msg.decode() if msg else ''}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().fp_engine_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_contig(self, cid: int, words: np.ndarray, n: int):
+        w = np.ascontiguousarray(words, dtype=np.uint32)
+        self._check(lib().fp_engine_set_contig(self.h, cid, w.ctypes.data, n), "set_contig")
+
+    def set_known_sites(self, cid: int, start: np.ndarray, stop: np.ndarray):
+        st = np.ascontiguousarray(start, dtype=np.uint32)
+        sp = np.ascontiguousarray(stop, dtype=np.uint32)
+        self._check(lib().fp_engine_set_known_sites(self.h, cid, st.ctypes.data, sp.ctypes.data, len(st)),
+                    "set_known_sites")
+
+    def load_reference(self, ref):
+        for cid, (words, n) in enumerate(ref.contigs):
+            self.set_contig(cid, words, n)
+            st, sp = ref.sites[cid]
+            self.set_known_sites(cid, st, sp)
+
+    def submit(self, batch):
+        v = batch.view(FpBatchView)
+        self._check(lib().fp_engine_submit_batch(self.h, C.byref(v)), "submit_batch")
+
+    def submit_view(self, view: FpBatchView):
+        self._check(lib().fp_engine_submit_batch(self.h, C.byref(view)), "submit_batch")
+
+    def submit_device_view(self, view: FpBatchView):
+        """Submits a batch whose arrays are device pointers (already resident in HBM)."""
+        self._check(lib().fp_engine_submit_batch_device(self.h, C.byref(view)), "submit_batch_device")
+
+    @property
+    def stream(self) -> int:
+        return lib().fp_engine_cuda_stream(self.h) or 0
+
+    def finalize(self) -> dict:
+        self._check(lib().fp_engine_finalize(self.h), "finalize")
+        out = {}
+        for t in range(4):
+            tv = FpTableView()
+            self._check(lib().fp_engine_get_table(self.h, t, C.byref(tv)), "get_table")
+            out[t] = table_to_numpy(tv)
+        return out
+
+    def write_report(self, path, rg_names, disable_rounding=False, version=(1, 1, 1)):
+        self._check(lib().fp_engine_write_report(self.h, str(path).encode(), _names(rg_names), len(rg_names),
+                                                 int(disable_rounding), *version), "write_report")
+
+    def reset(self):
+        self._check(lib().fp_engine_reset(self.h), "reset")
+
+    def stats(self) -> dict:
+        s = FpStats()
+        self._check(lib().fp_engine_get_stats(self.h, C.byref(s)), "get_stats")
+        d = {f: getattr(s, f) for f, _ in FpStats._fields_ if f != "gpu_ms_per_stage"}
+        d["gpu_ms_per_stage"] = list(s.gpu_ms_per_stage)
+        return d
+
+    def debug_last_batch(self, batch) -> dict:
+        R, Q = batch.num_reads, batch.num_qualities
+        d = {"read_status": np.zeros(R, np.uint8), "windows": np.zeros((R, 8), np.uint16),
+             "hmm": np.zeros((R, 4), np.int16), "base_flags": np.zeros(Q, np.uint8),
+             "baq_tag": np.zeros(Q, np.uint8), "frac_errors": np.zeros((Q, 3), np.float64)}
+        self._check(lib().fp_engine_debug_last_batch(self.h, *(d[k].ctypes.data for k in (
+            "read_status", "windows", "hmm", "base_flags", "baq_tag", "frac_errors"))), "debug_last_batch")
+        return d
+
+
+class PinnedBatch:
+    """A batch copied into page-locked host memory (fp_host_alloc) for full-speed H2D copies."""
+
+    def __init__(self, batch):
+        from .synth import BATCH_FIELDS, Batch
+        self._ptrs = []
+        arrays = {}
+        for name, dt, _ in BATCH_FIELDS:
+            a = batch.arrays[name]
+            p = C.c_void_p()
+            rc = lib().fp_host_alloc(max(1, a.nbytes), C.byref(p))
+            if rc != FP_OK:
+                raise EngineError("fp_host_alloc failed")
+            self._ptrs.append(p)
+            buf = (C.c_uint8 * max(1, a.nbytes)).from_address(p.value)
+            dst = np.frombuffer(buf, dtype=dt, count=len(a))
+            dst[:] = a
+            arrays[name] = dst
+        self.batch = Batch(arrays, batch.num_reads, batch.num_cigar_ops, batch.num_read_symbols, batch.num_qualities)
+        self.view = self.batch.view(FpBatchView)
+
+    def close(self):
+        for p in self._ptrs:
+            lib().fp_host_free(p)
+        self._ptrs = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,172 @@
+"""Hand-built alignment batch covering the reference's special cases: every read filter, clip layouts,
+leading/trailing insertions, deletions, '=' and X ops, N bases, low-quality tails, reads at both contig
+ends, adapter clipping of short fragments, wide bands, known sites under reads, and malformed input."""
+from __future__ import annotations
+
+import re
+
+import numpy as np
+
+from firepony_gb300.synth import Batch, pack4
+
+OPS = {"M": 0, "I": 1, "D": 2, "N": 3, "S": 4, "H": 5, "P": 6, "=": 7, "X": 8}
+IUPAC = {"A": 1, "C": 2, "G": 4, "T": 8, "N": 15}
+DNA = "ACGT"
+
+
+def make_reference(n=3000, seed=7):
+    rng = np.random.default_rng(seed)
+    seq = "".join(rng.choice(list(DNA), size=n))
+    return seq
+
+
+def parse_cigar(c):
+    return [(int(n), op) for n, op in re.findall(r"(\d+)([MIDNSHP=X])", c)]
+
+
+def read_from_cigar(ref, pos, cigar, rng, sub_positions=(), qual=30, n_at=()):
+    """Read bases following the CIGAR over ref[pos:], with substitutions at the given read offsets."""
+    seq = []
+    rp = pos
+    for n, op in parse_cigar(cigar):
+        for _ in range(n):
+            if op in "M=X":
+                seq.append(ref[rp] if rp < len(ref) else "A")
+                rp += 1
+            elif op in "IS":
+                seq.append(DNA[rng.integers(4)])
+            elif op in "DNHP":
+                if op in "DN":
+                    rp += 1
+    seq = list(seq)
+    for i in sub_positions:
+        if i < len(seq):
+            seq[i] = {"A": "C", "C": "G", "G": "T", "T": "A"}[seq[i]]
+    for i in n_at:
+        if i < len(seq):
+            seq[i] = "N"
+    quals = np.full(len(seq), qual, np.uint8)
+    span = sum(n for n, op in parse_cigar(cigar) if op in "M=XDN")
+    return "".join(seq), quals, span
+
+
+def build_batch(records):
+    """records: dicts with keys pos, cigar, seq, quals, flags, mapq, rg, chrom, mate_pos, isize."""
+    R = len(records)
+    chrom = np.array([r.get("chrom", 0) for r in records], np.uint16)
+    astart = np.array([r["pos"] for r in records], np.uint32)
+    astop = np.array([r["pos"] + max(r.get("span", 1), 1) - 1 for r in records], np.uint32)
+    mstart = np.array([r.get("mate_pos", 0) for r in records], np.uint32)
+    isize = np.array([r.get("isize", 0) for r in records], np.int32)
+    cig, cstart, clen = [], [], []
+    syms, rstart, rlen = [], [], []
+    quals, qstart, qlen = [], [], []
+    for r in records:
+        ops = parse_cigar(r["cigar"])
+        cstart.append(len(cig))
+        clen.append(len(ops))
+        cig.extend((n & 0xFFFFFF) | (OPS[op] << 24) for n, op in ops)
+        s = [IUPAC[c] for c in r["seq"]]
+        pad = (len(s) + 7) // 8 * 8
+        rstart.append(len(syms))
+        rlen.append(len(s))
+        syms.extend(s + [0] * (pad - len(s)))
+        q = list(r["quals"])
+        qstart.append(len(quals))
+        qlen.append(r.get("qual_len", len(q)))
+        quals.extend(q)
+    arrays = {
+        "chromosome": chrom, "alignment_start": astart, "alignment_stop": astop, "mate_alignment_start": mstart,
+        "inferred_insert_size": isize, "cigars": np.array(cig, np.uint32), "cigar_start": np.array(cstart, np.uint32),
+        "cigar_len": np.array(clen, np.uint32), "reads": pack4(np.array(syms, np.uint8)),
+        "read_start": np.array(rstart, np.uint32), "read_len": np.array(rlen, np.uint32),
+        "qualities": np.array(quals, np.uint8), "qual_start": np.array(qstart, np.uint32),
+        "qual_len": np.array(qlen, np.uint32), "flags": np.array([r.get("flags", 0) for r in records], np.uint16),
+        "mapq": np.array([r.get("mapq", 60) for r in records], np.uint8),
+        "read_group": np.array([r.get("rg", 0) for r in records], np.uint32),
+    }
+    return Batch(arrays, R, len(cig), len(syms), len(quals))
+
+
+def edge_case_dataset(seed=11):
+    """Returns (contigs, sites, batch): contigs as [(words, n)], sites as [(start, stop)]."""
+    rng = np.random.default_rng(seed)
+    ref = make_reference(3000, seed)
+    L = len(ref)
+    recs = []
+
+    def add(pos, cigar, subs=(), flags=0, mapq=60, rg=0, qual=30, quals=None, n_at=(), chrom=0, mate_pos=0,
+            isize=0, qual_len=None):
+        seq, q, span = read_from_cigar(ref, pos, cigar, rng, subs, qual, n_at)
+        if quals is not None:
+            q = np.array(quals, np.uint8)[:len(seq)]
+        rec = dict(pos=pos, cigar=cigar, seq=seq, quals=q, flags=flags, mapq=mapq, rg=rg, chrom=chrom,
+                   mate_pos=mate_pos, isize=isize, span=span)
+        if qual_len is not None:
+            rec["qual_len"] = qual_len
+        recs.append(rec)
+
+    REV, PAIRED, READ2, MREV = 16, 1, 128, 32
+    add(100, "50M", subs=(10, 30))
+    add(120, "50M", subs=(5,), flags=REV)
+    add(140, "5S40M5S", subs=(20,))
+    add(160, "3H47M", subs=(12,))
+    add(180, "47M3H", subs=(40,), flags=REV)
+    add(200, "10M2I38M", subs=(25,))
+    add(220, "10M2I38M", subs=(25,), flags=REV)
+    add(240, "10M3D40M", subs=(35,))
+    add(260, "10M3D40M", subs=(35,), flags=REV)
+    add(280, "2I48M", subs=(30,))
+    add(300, "48M2I", subs=(20,), flags=REV)
+    add(320, "5S2I43M", subs=(15,))
+    add(340, "2D48M", subs=(22,))
+    add(360, "20M1D1I29M", subs=(3,))
+    add(380, "20=5X25M", subs=(21, 40))
+    add(400, "50M", subs=(12,), n_at=(25,))
+    add(420, "50M", subs=(12,), quals=[30] * 10 + [4] * 5 + [30] * 33 + [2, 2])
+    add(440, "50M", subs=(12,), quals=[2, 2, 2] + [25] * 47)
+    add(460, "50M", mapq=0)
+    add(480, "50M", mapq=255)
+    add(500, "50M", flags=1024)
+    add(520, "50M", flags=512)
+    add(540, "50M", flags=256)
+    add(560, "50M", flags=4)
+    add(580, "20M5N30M")
+    add(600, "10M5S10M")
+    add(620, "5H5S40M", subs=(10,))
+    add(640, "5S5H40M")
+    add(0, "50M", subs=(10,))
+    add(1, "50M", subs=(10,), flags=REV)
+    add(2, "3S47M", subs=(10,))
+    add(L - 50, "50M", subs=(10,))
+    add(L - 48, "48M", subs=(10,), flags=REV)
+    add(L - 20, "40M", subs=(5,))
+    add(L - 60, "50M", subs=(10,))
+    add(700, "50M", subs=(10, 45), flags=PAIRED | MREV, mate_pos=705, isize=40)
+    add(705, "50M", subs=(3, 44), flags=PAIRED | REV | READ2, mate_pos=700, isize=-40)
+    add(740, "5S45M", subs=(10,), flags=PAIRED | MREV, mate_pos=760, isize=60)
+    add(760, "45M5S", subs=(30,), flags=PAIRED | REV | READ2, mate_pos=740, isize=-60)
+    add(800, "50M", rg=0xFFFFFFFF)
+    add(820, "30M15D20M", subs=(10, 40))
+    add(860, "25M10D25M", subs=(5, 30), flags=REV)
+    add(900, "1M")
+    add(910, "50M", chrom=5)
+    add(920, "50M", qual_len=40)
+    add(1000, "150M", subs=(20, 70, 140))
+    add(1200, "60M", subs=(0, 59))
+    add(1300, "30M4I30M", subs=(31, 32))
+    add(1400, "40M", quals=[40] * 40)
+    add(1500, "100M", subs=tuple(range(0, 100, 7)), flags=PAIRED | READ2)
+    add(1650, "511M", subs=(100, 300, 500)) if L > 2200 else None
+    add(1800, "70M", subs=(35,), rg=1)
+    add(1850, "70M", subs=(35,), rg=2, flags=REV)
+
+    # known sites: SNPs under reads 0, 5, 9; an indel site; a site at the read edge
+    sites = sorted([(110, 110), (130, 130), (215, 215), (245, 247), (289, 289), (1010, 1012), (1220, 1220),
+                    (1259, 1259), (1815, 1815)])
+    batch = build_batch(recs)
+    seq_syms = np.array([IUPAC[c] for c in ref], np.uint8)
+    contigs = [(pack4(seq_syms), L)]
+    st = np.array([s for s, _ in sites], np.uint32)
+    sp = np.array([e for _, e in sites], np.uint32)
+    return contigs, [(st, sp)], batch, 3

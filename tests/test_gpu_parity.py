@@ -1,0 +1,197 @@
+"""GPU parity: the CUDA engine (through the C ABI) against the oracle on the same seeded inputs.
+
+Bar: covariate keys, observation counts, float mismatch sums and empirical qualities bit-exact; expected
+errors and estimated qualities within 1e-9 relative (CUDA log10 vs libm on the rounded-prior tables);
+per-stage intermediates (read status, windows, HMM window/band width, error and mask bits, BQ tags,
+fractional errors) identical for every active read."""
+import numpy as np
+import pytest
+
+from tests.conftest import make_dataset
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-9
+
+
+def run_engine(ref_or_contigs, batches, n_rg, mode, sites=None):
+    from firepony_gb300.engine import Engine
+    e = Engine(num_read_groups=n_rg, baq_mode=mode)
+    if sites is None:
+        e.load_reference(ref_or_contigs)
+    else:
+        for cid, (w, n) in enumerate(ref_or_contigs):
+            e.set_contig(cid, w, n)
+        for cid, (st, sp) in enumerate(sites):
+            e.set_known_sites(cid, st, sp)
+    dbg = None
+    for b in batches:
+        e.submit(b)
+        dbg = e.debug_last_batch(b)
+    tables = e.finalize()
+    stats = e.stats()
+    e.close()
+    return tables, stats, dbg
+
+
+def run_oracle(ref_or_contigs, batches, n_rg, sites=None):
+    from oracle.oracle import Oracle
+    o = Oracle(n_rg)
+    if sites is None:
+        o.load_reference(ref_or_contigs)
+    else:
+        from oracle.oracle import lib
+        for cid, (w, n) in enumerate(ref_or_contigs):
+            w = np.ascontiguousarray(w, np.uint32)
+            lib().fpo_set_contig(o.h, cid, w.ctypes.data, n)
+        for cid, (st, sp) in enumerate(sites):
+            st = np.ascontiguousarray(st, np.uint32)
+            sp = np.ascontiguousarray(sp, np.uint32)
+            lib().fpo_set_known_sites(o.h, cid, st.ctypes.data, sp.ctypes.data, len(st))
+    dbg = None
+    for b in batches:
+        o.process(b)
+        dbg = o.debug_last_batch(b)
+    tables = o.finalize()
+    return tables, o.stats(), dbg
+
+
+def assert_tables_equal(a, b):
+    for t in range(4):
+        ta, tb = a[t], b[t]
+        assert len(ta["keys"]) == len(tb["keys"]), f"table {t}: {len(ta['keys'])} vs {len(tb['keys'])} rows"
+        np.testing.assert_array_equal(ta["keys"], tb["keys"], err_msg=f"table {t} keys")
+        np.testing.assert_array_equal(ta["observations"], tb["observations"], err_msg=f"table {t} observations")
+        np.testing.assert_array_equal(ta["mismatches"], tb["mismatches"], err_msg=f"table {t} mismatches")
+        np.testing.assert_array_equal(ta["empirical_quality"], tb["empirical_quality"],
+                                      err_msg=f"table {t} empirical quality")
+        np.testing.assert_allclose(ta["expected_errors"], tb["expected_errors"], rtol=REL_TOL, atol=0)
+        np.testing.assert_allclose(ta["estimated_quality"], tb["estimated_quality"], rtol=REL_TOL, atol=0)
+
+
+def assert_stages_equal(batch, ge, go):
+    st_e, st_o = ge["read_status"], go["read_status"]
+    np.testing.assert_array_equal(st_e, st_o, err_msg="read status")
+    act = st_o == 1
+    np.testing.assert_array_equal(ge["windows"][act][:, :6], go["windows"][act][:, :6], err_msg="windows")
+    np.testing.assert_array_equal(ge["windows"][act][:, 6:], go["windows"][act][:, 6:], err_msg="hq windows")
+    np.testing.assert_array_equal(ge["hmm"][act], go["hmm"][act], err_msg="hmm window / band / errors")
+    qs, ql = batch["qual_start"], batch["qual_len"]
+    mask = np.zeros(batch.num_qualities, bool)
+    for r in np.nonzero(act)[0]:
+        mask[qs[r]:qs[r] + ql[r]] = True
+    np.testing.assert_array_equal(ge["base_flags"][mask], go["base_flags"][mask], err_msg="base flags")
+    np.testing.assert_array_equal(ge["baq_tag"][mask], go["baq_tag"][mask], err_msg="BQ tags")
+    # fractional errors inside the clipped windows (the engine stores them as the table's float values)
+    win = np.zeros(batch.num_qualities, bool)
+    for r in np.nonzero(act)[0]:
+        x, y = go["windows"][r][0], go["windows"][r][1]
+        win[qs[r] + x:qs[r] + y + 1] = True
+    fo = go["frac_errors"][win].astype(np.float32).astype(np.float64)
+    np.testing.assert_array_equal(ge["frac_errors"][win], fo, err_msg="fractional errors")
+
+
+@pytest.mark.parametrize("mode", ["fp32", "fp64"])
+@pytest.mark.parametrize("preset,n,batch,refbp", [
+    ("plain_100k_101bp", 6000, 2000, 200_000),
+    ("precision_20M_151bp_pe", 6000, 3000, 400_000),
+    ("batched_uneven", 6000, 1500, 400_000),
+])
+def test_tables_match_oracle(native, preset, n, batch, refbp, mode):
+    p, ref, batches = make_dataset(preset, n, batch, refbp)
+    te, se, ge = run_engine(ref, batches, p.num_read_groups, mode)
+    to, so, go = run_oracle(ref, batches, p.num_read_groups)
+    assert se["total_reads"] == so["total_reads"]
+    assert se["filtered_reads"] == so["filtered_reads"]
+    assert se["baq_reads"] == so["baq_reads"]
+    assert_stages_equal(batches[-1], ge, go)
+    assert_tables_equal(te, to)
+
+
+@pytest.mark.parametrize("mode", ["fp32", "fp64"])
+def test_edge_cases_match_oracle(native, mode):
+    from tests.edge_cases import edge_case_dataset
+    contigs, sites, batch, n_rg = edge_case_dataset()
+    te, se, ge = run_engine(contigs, [batch], n_rg, mode, sites)
+    to, so, go = run_oracle(contigs, [batch], n_rg, sites)
+    assert se["filtered_reads"] == so["filtered_reads"]
+    assert_stages_equal(batch, ge, go)
+    assert_tables_equal(te, to)
+
+
+def test_fp32_and_fp64_paths_agree(native):
+    p, ref, batches = make_dataset("precision_20M_151bp_pe", 20000, 10000, 1_000_000)
+    t32, s32, _ = run_engine(ref, batches, p.num_read_groups, "fp32")
+    t64, s64, _ = run_engine(ref, batches, p.num_read_groups, "fp64")
+    assert_tables_equal(t32, t64)
+    # escalation is the exception, not the rule
+    assert s32["baq_fp64_escalated_reads"] < 0.25 * s32["baq_reads"]
+
+
+def test_batch_size_independent(native):
+    """The canonical summation order makes the tables independent of how reads are batched."""
+    p, ref, batches = make_dataset("plain_100k_101bp", 8000, 8000, 200_000)
+    whole = batches[0]
+    parts = [whole.subset(np.arange(i, min(i + 1500, whole.num_reads))) for i in range(0, whole.num_reads, 1500)]
+    t1, _, _ = run_engine(ref, [whole], p.num_read_groups, "fp32")
+    t2, _, _ = run_engine(ref, parts, p.num_read_groups, "fp32")
+    assert_tables_equal(t1, t2)
+
+
+def test_report_identical(native, tmp_path):
+    from firepony_gb300.engine import Engine, write_report
+    p, ref, batches = make_dataset("precision_20M_151bp_pe", 4000, 2000, 300_000)
+    e = Engine(num_read_groups=p.num_read_groups)
+    e.load_reference(ref)
+    for b in batches:
+        e.submit(b)
+    e.finalize()
+    names = [f"rg{i}" for i in range(p.num_read_groups)]
+    e.write_report(tmp_path / "gpu.txt", names)
+    e.close()
+    to, _, _ = run_oracle(ref, batches, p.num_read_groups)
+    write_report(tmp_path / "oracle.txt", to, names)
+    assert (tmp_path / "gpu.txt").read_bytes() == (tmp_path / "oracle.txt").read_bytes()
+
+
+def test_bad_input_rejected_and_engine_usable(native):
+    from firepony_gb300.engine import Engine, EngineError
+    p, ref, batches = make_dataset("plain_100k_101bp", 500, 500, 100_000)
+    e = Engine(num_read_groups=1)
+    e.load_reference(ref)
+    bad = batches[0].subset(np.arange(500))
+    bad.arrays["read_group"][3] = 7  # >= num_read_groups
+    with pytest.raises(EngineError, match="BAD_INPUT"):
+        e.submit(bad)
+    bad2 = batches[0].subset(np.arange(500))
+    bad2.arrays["read_start"][5] = 10**9  # outside the batch arrays
+    with pytest.raises(EngineError, match="BAD_INPUT"):
+        e.submit(bad2)
+    e.submit(batches[0])
+    t = e.finalize()
+    e.close()
+    to, _, _ = run_oracle(ref, batches, 1)
+    assert_tables_equal(t, to)
+
+
+def test_large_batch_properties(native):
+    """Size-independent properties at a full-size batch (1M reads of 151 bp)."""
+    from firepony_gb300.engine import Engine
+    p, ref, batches = make_dataset("precision_20M_151bp_pe", 1_000_000, 1_000_000, 50_000_000)
+    e = Engine(num_read_groups=p.num_read_groups)
+    e.load_reference(ref)
+    e.submit(batches[0])
+    t = e.finalize()
+    s = e.stats()
+    e.close()
+    q = t[1]
+    ev = q["keys"] & 3
+    # every gathered base adds one observation to its M, I and D quality keys
+    m, i, d = (q["observations"][ev == k].sum() for k in range(3))
+    assert m == i == d > 0
+    # read-group rows sum the quality rows
+    assert t[0]["observations"].sum() == q["observations"].sum()
+    # keys ascend
+    for k in range(4):
+        assert np.all(np.diff(t[k]["keys"].astype(np.int64)) > 0)
+    assert s["total_reads"] == 1_000_000
