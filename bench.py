@@ -84,7 +84,7 @@ class ClockSampler:
         sm = sorted(float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit())
         mx = max((float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()), default=None)
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples for i in range(4) if "Active" in s[3 + i]})
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].strip() == "Active"})
         return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons,
                 "samples": len(self.samples)}
 
@@ -272,7 +272,8 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    res = run_gb300(args, rank % max(1, int(os.environ.get("LOCAL_WORLD_SIZE", "1")) if world > 1 else 0, world)
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    res = run_gb300(args, local_rank, world)
     import torch
     ms = res["ms_value"]
     t_e2e = res["t_e2e"]
