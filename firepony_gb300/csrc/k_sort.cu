@@ -4,6 +4,7 @@
 // the running total reproduces the reference's append + stable sort + reduce_by_key of every batch
 // (device/covariates.cu:172-201, device/covariate_table.cu:43-107) as one sequential float sum per key.
 #include "kernels.h"
+#include "firepony_gb300.h"
 
 namespace fpg {
 
@@ -252,4 +253,55 @@ void launch_fold(const u64 *sorted, u64 n, float *mism, void *tmp, cudaStream_t 
     g_kernel_launches += 3;
 }
 
+// ---- C ABI: the radix sort as a standalone primitive ----
+namespace {
+
+// Runs the LSD passes so that the last pass lands in `out`; the first pass reads `in` and never writes it.
+void sort_into(const u64 *in, u64 *out, u64 *alt, u64 n, int key_bits, void *tmp, cudaStream_t s) {
+    int passes = 0;
+    for (int shift = 0; shift < key_bits; shift += 8) passes++;
+    if (n <= 1 || passes == 0) {
+        if (n) cudaMemcpyAsync(out, in, n * sizeof(u64), cudaMemcpyDeviceToDevice, s);
+        return;
+    }
+    const u32 nblocks = u32((n + RS_TILE - 1) / RS_TILE);
+    const u64 hist_n = u64(nblocks) * 256;
+    u32 *hist = reinterpret_cast<u32 *>(tmp);
+    u32 *offs = hist + hist_n + 1;
+    void *stmp = offs + hist_n + 1;
+    const u64 *src = in;
+    int p = 0;
+    for (int shift = 0; shift < key_bits; shift += 8, p++) {
+        // pass p writes `out` when the number of passes left (passes - p) is odd
+        u64 *dst = ((passes - p) % 2 == 1) ? out : alt;
+        k_rs_hist<<<nblocks, RS_THREADS, 0, s>>>(src, n, shift, hist, nblocks);
+        scan_rec(hist, offs, hist_n, reinterpret_cast<u32 *>(stmp), s);
+        k_rs_scatter<<<nblocks, RS_THREADS, 0, s>>>(src, n, shift, offs, nblocks, dst);
+        g_kernel_launches += 2;
+        src = dst;
+    }
+}
+
+}  // namespace
+
 }  // namespace fpg
+
+extern "C" fp_status fp_sort_entries(const uint64_t *d_in, uint64_t *d_out, uint64_t n, int key_bits, void *stream) {
+    using namespace fpg;
+    if ((!d_in || !d_out) && n) return FP_BAD_INPUT;
+    if (key_bits < 0 || key_bits > 32) return FP_BAD_INPUT;
+    if (n == 0) return FP_OK;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const size_t tmp_bytes = radix_tmp_bytes(n);
+    void *tmp = nullptr, *alt = nullptr;
+    if (cudaMallocAsync(&tmp, tmp_bytes, s) != cudaSuccess) return FP_OOM;
+    if (cudaMallocAsync(&alt, n * sizeof(u64), s) != cudaSuccess) {
+        cudaFreeAsync(tmp, s);
+        return FP_OOM;
+    }
+    sort_into(reinterpret_cast<const u64 *>(d_in), reinterpret_cast<u64 *>(d_out), reinterpret_cast<u64 *>(alt), n,
+              key_bits, tmp, s);
+    cudaFreeAsync(alt, s);
+    cudaFreeAsync(tmp, s);
+    return cudaGetLastError() == cudaSuccess ? FP_OK : FP_DEVICE_ERROR;
+}

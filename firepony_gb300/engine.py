@@ -20,7 +20,7 @@ EXPORTED = [
     "fp_engine_create", "fp_engine_destroy", "fp_last_error", "fp_engine_set_contig", "fp_engine_set_known_sites",
     "fp_engine_submit_batch", "fp_engine_finalize", "fp_engine_get_table", "fp_engine_write_report",
     "fp_engine_reset", "fp_engine_get_stats", "fp_engine_debug_last_batch", "fp_report_write", "fp_host_alloc",
-    "fp_host_free", "fp_engine_submit_batch_device", "fp_engine_cuda_stream",
+    "fp_host_free", "fp_engine_submit_batch_device", "fp_engine_cuda_stream", "fp_sort_entries",
 ]
 
 
@@ -60,6 +60,7 @@ def lib():
         L.fp_engine_submit_batch_device.argtypes = [C.c_void_p, C.POINTER(FpBatchView)]
         L.fp_engine_cuda_stream.restype = C.c_void_p
         L.fp_engine_cuda_stream.argtypes = [C.c_void_p]
+        L.fp_sort_entries.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_int, C.c_void_p]
         L.fp_host_alloc.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
         L.fp_host_free.argtypes = [C.c_void_p]
         _lib = L
@@ -92,6 +93,13 @@ def write_report(path, tables: dict, rg_names, disable_rounding=False, version=(
                                *version)
     if rc != FP_OK:
         raise EngineError(f"fp_report_write: {STATUS_NAMES.get(rc, rc)}")
+
+
+def sort_entries(d_in: int, d_out: int, n: int, key_bits: int, stream: int = 0) -> None:
+    """fp_sort_entries on device pointers (stable radix sort of packed 64-bit entries by bits 32..)."""
+    rc = lib().fp_sort_entries(d_in, d_out, n, key_bits, stream or None)
+    if rc != FP_OK:
+        raise EngineError(f"fp_sort_entries: {STATUS_NAMES.get(rc, rc)}")
 
 
 class Engine:

@@ -181,6 +181,13 @@ fp_status fp_engine_debug_last_batch(fp_engine *engine, uint8_t *read_status, ui
                                      int16_t *hmm, uint8_t *base_flags, uint8_t *baq_tag,
                                      double *frac_errors);
 
+/* Stable LSD radix sort of n packed 64-bit covariate entries (key in bits 32..63, payload below) by key
+ * bits [32, 32 + key_bits), device pointers in and out (d_in is not modified; the ranges must not
+ * overlap). The engine's K4 sort, exposed for callers that build their own entry streams, in the role of
+ * covariate_table::sort (device/covariate_table.cu:43-57). Runs on `stream` (a cudaStream_t, NULL for the
+ * default stream) and returns once the work is queued; scratch is allocated and freed on that stream. */
+fp_status fp_sort_entries(const uint64_t *d_in, uint64_t *d_out, uint64_t n, int key_bits, void *stream);
+
 /* Writes a GATKReport from four table views (indexed by fp_table_id); the same writer as
  * fp_engine_write_report, usable on any tables in this layout. */
 fp_status fp_report_write(const char *path, const fp_table_view *tables, const char *const *rg_names,
