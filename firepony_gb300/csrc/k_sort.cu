@@ -3,6 +3,8 @@
 // table. Stable sorting keeps each key's entries in stream order, so folding a segment left to right from
 // the running total reproduces the reference's append + stable sort + reduce_by_key of every batch
 // (device/covariates.cu:172-201, device/covariate_table.cu:43-107) as one sequential float sum per key.
+#include <mutex>
+
 #include "kernels.h"
 #include "firepony_gb300.h"
 
@@ -303,5 +305,64 @@ extern "C" fp_status fp_sort_entries(const uint64_t *d_in, uint64_t *d_out, uint
               key_bits, tmp, s);
     cudaFreeAsync(alt, s);
     cudaFreeAsync(tmp, s);
+    return cudaGetLastError() == cudaSuccess ? FP_OK : FP_DEVICE_ERROR;
+}
+
+// ---- allocation-free variant ----
+// Some callers cannot allocate device memory while they run: a serving loop that admits jobs against a
+// fixed HBM budget (an allocation mid-job would break its accounting), or a host framework that owns all
+// device memory through its own pool and forbids driver allocations. fp_sort_entries_static serves them
+// from a fixed scratch array that lives in the library image, sized for at most FP_STATIC_SORT_MAX entries.
+namespace fpg {
+namespace {
+
+constexpr u64 STATIC_SORT_MAX = u64(1) << 20;
+constexpr size_t STATIC_ALT_BYTES = size_t(STATIC_SORT_MAX) * sizeof(u64);
+constexpr size_t STATIC_TMP_BYTES = size_t(5) << 18;  // 1.25 MiB: histograms, offsets and scan sums
+
+// Every GPU that loads the library holds this array (about 9.25 MiB) until the process exits. All calls
+// share it: calls whose work overlaps on the GPU (different streams, or different host threads) race on it.
+static __device__ __align__(256) unsigned char g_static_sort_scratch[STATIC_ALT_BYTES + STATIC_TMP_BYTES];
+
+std::mutex g_static_mu;
+void *g_static_addr[64] = {};
+
+// Device address of the scratch array on the current device, looked up once per device (host code only
+// sees a stand-in for the symbol; the kernels must be given this address).
+cudaError_t static_scratch(void **out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_addr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_static_sort_scratch);
+        if (e != cudaSuccess) return e;
+        g_static_addr[dev] = p;
+    }
+    *out = g_static_addr[dev];
+    return cudaSuccess;
+}
+
+}  // namespace
+}  // namespace fpg
+
+extern "C" fp_status fp_sort_entries_static(const uint64_t *d_in, uint64_t *d_out, uint64_t n, int key_bits,
+                                            void *stream) {
+    using namespace fpg;
+    if ((!d_in || !d_out) && n) return FP_BAD_INPUT;
+    if (key_bits < 0 || key_bits > 32) return FP_BAD_INPUT;
+    if (n > STATIC_SORT_MAX) return FP_BAD_INPUT;
+    if (radix_tmp_bytes(STATIC_SORT_MAX) > STATIC_TMP_BYTES) return FP_DEVICE_ERROR;
+    if (n == 0) return FP_OK;
+    void *scratch = nullptr;
+    if (static_scratch(&scratch) != cudaSuccess) return FP_DEVICE_ERROR;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    u64 *alt = reinterpret_cast<u64 *>(scratch);
+    void *tmp = static_cast<unsigned char *>(scratch) + STATIC_ALT_BYTES;
+    // nothing in the scratch needs clearing: every histogram, offset and scan entry a pass reads is
+    // written earlier in the same pass
+    sort_into(reinterpret_cast<const u64 *>(d_in), reinterpret_cast<u64 *>(d_out), alt, n, key_bits, tmp, s);
     return cudaGetLastError() == cudaSuccess ? FP_OK : FP_DEVICE_ERROR;
 }

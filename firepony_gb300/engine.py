@@ -21,6 +21,7 @@ EXPORTED = [
     "fp_engine_submit_batch", "fp_engine_finalize", "fp_engine_get_table", "fp_engine_write_report",
     "fp_engine_reset", "fp_engine_get_stats", "fp_engine_debug_last_batch", "fp_report_write", "fp_host_alloc",
     "fp_host_free", "fp_engine_submit_batch_device", "fp_engine_cuda_stream", "fp_sort_entries",
+    "fp_sort_entries_static",
 ]
 
 
@@ -61,6 +62,7 @@ def lib():
         L.fp_engine_cuda_stream.restype = C.c_void_p
         L.fp_engine_cuda_stream.argtypes = [C.c_void_p]
         L.fp_sort_entries.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_int, C.c_void_p]
+        L.fp_sort_entries_static.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_int, C.c_void_p]
         L.fp_host_alloc.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
         L.fp_host_free.argtypes = [C.c_void_p]
         _lib = L

@@ -188,6 +188,15 @@ fp_status fp_engine_debug_last_batch(fp_engine *engine, uint8_t *read_status, ui
  * default stream) and returns once the work is queued; scratch is allocated and freed on that stream. */
 fp_status fp_sort_entries(const uint64_t *d_in, uint64_t *d_out, uint64_t n, int key_bits, void *stream);
 
+/* fp_sort_entries without any device allocation, for callers that must not allocate while they run (a
+ * serving loop admitting jobs against a fixed HBM budget, or a host framework whose own pool owns all device
+ * memory). No counterpart in the reference. Scratch is a fixed array inside the library (about 9.25 MiB per
+ * GPU, held until the process exits); n may be at most FP_STATIC_SORT_MAX, larger n returns FP_BAD_INPUT.
+ * The first call on a device looks up that device's scratch address: make it before any stream capture.
+ * All calls share the scratch, so calls whose work overlaps on the GPU race; serialise them. */
+#define FP_STATIC_SORT_MAX (1u << 20)
+fp_status fp_sort_entries_static(const uint64_t *d_in, uint64_t *d_out, uint64_t n, int key_bits, void *stream);
+
 /* Writes a GATKReport from four table views (indexed by fp_table_id); the same writer as
  * fp_engine_write_report, usable on any tables in this layout. */
 fp_status fp_report_write(const char *path, const fp_table_view *tables, const char *const *rg_names,
