@@ -88,17 +88,21 @@ __device__ __forceinline__ u32 op_code(u32 c) { return (c >> 24) & 0xFu; }
 // The engine accumulates the three observation tables in dense arrays whose index is a monotone function
 // of the reference's 32-bit key, so ascending dense index == ascending key (the reduced tables' order,
 // device/covariate_table.cu:43-107):
-//   quality: ((rg*256 + q) * 3 + ev)
-//   cycle:   ((rg*256 + q) * 1024 + cycle_field) * 3 + ev
-//   context: ((rg*256 + q) * 80 + context_rank) * 3 + ev
-// context_rank enumerates the 80 context values that can occur in a valid key, (c<<4)|2 for 2-mers and
-// (c<<4)|3 for 3-mers, in ascending order.
+//   quality: ((rg*256 + q) * 4 + slot)
+//   cycle:   ((rg*256 + q) * 1024 + cycle_field) * 4 + slot
+//   context: ((rg*256 + q) * 80 + context_rank) * 4 + slot
+// with event slots M -> 0, I -> 2, D -> 3 (slot 1 unused) so that the I and D counters of one prefix form
+// an aligned 8-byte pair. context_rank enumerates the 80 context values that can occur in a valid key,
+// (c<<4)|2 for 2-mers and (c<<4)|3 for 3-mers, in ascending order.
 constexpr u32 Q_SPAN = 256;
 constexpr u32 CYCLE_SPAN = 1024;
 constexpr u32 CONTEXT_SPAN = 80;
-constexpr u32 QUAL_KEYS_PER_RG = Q_SPAN * 3;
-constexpr u32 CYCLE_KEYS_PER_RG = Q_SPAN * CYCLE_SPAN * 3;
-constexpr u32 CONTEXT_KEYS_PER_RG = Q_SPAN * CONTEXT_SPAN * 3;
+constexpr u32 EV_SLOTS = 4;
+constexpr u32 QUAL_KEYS_PER_RG = Q_SPAN * EV_SLOTS;
+constexpr u32 CYCLE_KEYS_PER_RG = Q_SPAN * CYCLE_SPAN * EV_SLOTS;
+constexpr u32 CONTEXT_KEYS_PER_RG = Q_SPAN * CONTEXT_SPAN * EV_SLOTS;
+__host__ __device__ inline u32 ev_slot(u32 ev) { return ev == 0 ? 0u : ev + 1u; }
+__host__ __device__ inline u32 slot_ev(u32 slot) { return slot == 0 ? 0u : slot - 1u; }
 constexpr u32 CYCLE_INVALID = (1u << 10) - 1;
 constexpr u32 CONTEXT_INVALID = (1u << 11) - 1;
 

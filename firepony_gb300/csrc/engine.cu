@@ -93,7 +93,8 @@ struct fp_engine {
 
     // tables
     Tables tables{};
-    DevBuf tab_obs, tab_mism;
+    DevBuf tab_obs, tab_mism, tab_stage;
+    u64 staged_bases = 0;  // bases counted into the u32 stage since the last merge
 
     // batch buffers
     DevBuf in_buf;
@@ -140,6 +141,10 @@ fp_status alloc_tables(fp_engine *eng) {
     const size_t n = eng->tables.ks.total;
     CK(eng->tab_obs.ensure(n * sizeof(unsigned long long)), "table allocation");
     CK(eng->tab_mism.ensure(n * sizeof(float)), "table allocation");
+    CK(eng->tab_stage.ensure(n * sizeof(u32)), "table allocation");
+    CK(cudaMemsetAsync(eng->tab_stage.p, 0, n * sizeof(u32), eng->st), "table clear");
+    eng->tables.stage = eng->tab_stage.as<u32>();
+    eng->staged_bases = 0;
     CK(cudaMemsetAsync(eng->tab_obs.p, 0, n * sizeof(unsigned long long), eng->st), "table clear");
     CK(cudaMemsetAsync(eng->tab_mism.p, 0, n * sizeof(float), eng->st), "table clear");
     eng->tables.obs = eng->tab_obs.as<unsigned long long>();
@@ -194,6 +199,7 @@ fp_status fp_engine_create(const fp_options *o, fp_engine **out) {
     eng->hmm.gap_open = pow(10.0, (-40.0) / 10.);
     baq64_set_constants(eng->hmm);
     baq32_set_constants(eng->hmm);
+    baq_tpr_set_constants(eng->hmm);
     EmpConst ec;
     for (int d = 0; d <= 40; d++) ec.prior[d] = log10(gaussian(double(d)));
     for (int bin = 0; bin <= 60; bin++) {
@@ -223,7 +229,7 @@ void fp_engine_destroy(fp_engine *eng) {
     if (eng->st) cudaStreamSynchronize(eng->st);
     for (auto &b : eng->contig_bufs) b.release();
     for (auto &b : eng->site_bufs) b.release();
-    DevBuf *bufs[] = {&eng->d_contigs, &eng->d_sites, &eng->tab_obs, &eng->tab_mism, &eng->in_buf, &eng->oplen,
+    DevBuf *bufs[] = {&eng->d_contigs, &eng->d_sites, &eng->tab_obs, &eng->tab_mism, &eng->tab_stage, &eng->in_buf, &eng->oplen,
                       &eng->cigoff, &eng->ev_rc, &eng->ev_type, &eng->per_read, &eng->per_base, &eng->lists,
                       &eng->counters, &eng->entry_cnt, &eng->entry_off, &eng->entries, &eng->entries_alt,
                       &eng->sort_tmp, &eng->scan_tmp, &eng->s32, &eng->s64};
@@ -413,7 +419,7 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
         w.baq_state = reinterpret_cast<u32 *>(p); p += al(Q * 4);
         w.frac = reinterpret_cast<float *>(p);
     }
-    CK(eng->lists.ensure(al(R * 4ull) * 4), "work lists");
+    CK(eng->lists.ensure(al(R * 4ull) * 5), "work lists");
     w.baq_list = eng->lists.as<u32>();
     w.esc_list = w.baq_list + 3ull * R;
     CK(eng->entry_cnt.ensure(al((R + 1) * 4ull)), "entry counts");
@@ -452,26 +458,43 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
             if ((s = run_fp64(w.baq_list + size_t(c) * R, w.counters + c, n_cls[c], bw_max[c])) != FP_OK) return s;
         }
     } else {
-        const u64 s32_need = std::max(baq32_scratch_floats(16, 512), baq32_scratch_floats(32, 512));
-        CK(eng->s32.ensure(s32_need * 4), "FP32 BAQ scratch");
-        if (n_cls[0]) launch_baq32(b, eng->ref, w, w.baq_list, w.counters + 0, n_cls[0], 16, eng->s32.as<float>(), 512, st);
-        if (n_cls[1])
-            launch_baq32(b, eng->ref, w, w.baq_list + size_t(R), w.counters + 1, n_cls[1], 32, eng->s32.as<float>(), 512, st);
-        if (n_cls[0]) launch_cap(b, w, w.baq_list, w.counters + 0, 0, st, n_cls[0]);
-        if (n_cls[1]) launch_cap(b, w, w.baq_list + size_t(R), w.counters + 1, 0, st, n_cls[1]);
+        // FP32 with certified bounds (band classes 0 and 1), exact FP64 replay of the undecided reads, and the
+        // thread-per-read FP64 kernel for bands wider than 15
+        const u64 budget = u64(3) << 30;
+        CK(eng->s32.ensure(budget), "BAQ scratch");
+        for (int c = 0; c < 2; c++) {
+            if (!n_cls[c]) continue;
+            launch_baq_tpr(b, eng->ref, w, w.baq_list + size_t(c) * R, w.counters + c, n_cls[c], c, false,
+                           w.counters + 8 + c, eng->s32.p, budget, max_q, st);
+            launch_cap(b, w, w.baq_list + size_t(c) * R, w.counters + c, 0, st, n_cls[c]);
+        }
+        for (int c = 0; c < 2; c++) {
+            if (!n_cls[c]) continue;
+            const u32 *esc = w.esc_list + size_t(c) * R;
+            u32 *esc_count = w.counters + (c ? 10 : 4);
+            launch_baq_tpr(b, eng->ref, w, esc, esc_count, n_cls[c], c, true, w.counters + 11, eng->s32.p, budget,
+                           max_q, st);
+            launch_cap(b, w, esc, esc_count, 1, st, n_cls[c]);
+        }
         if ((s = run_fp64(w.baq_list + 2ull * R, w.counters + 2, n_cls[2], bw_max[2])) != FP_OK) return s;
-        // escalated reads (at most the class 0 and 1 reads)
-        if ((s = run_fp64(w.esc_list, w.counters + 4, n_cls[0] + n_cls[1], std::max(bw_max[0], bw_max[1]))) != FP_OK)
-            return s;
     }
     cudaEventRecord(eng->ev[4], st);
 
     // ---- K3 count + scan ----
+    // observation counts go to u32 stage counters; a key gains at most one count per base of the batch, so the
+    // stage is merged into the u64 table before the bases counted since the last merge could reach 2^32
+    if (eng->staged_bases + Q > 0xFFFFFFFFull) {
+        launch_merge_stage(eng->tables, st);
+        eng->staged_bases = 0;
+    }
+    eng->staged_bases += Q;
     launch_cov_count(b, w, eng->tables, st);
     launch_exclusive_scan(w.entry_count, w.entry_offset, R, eng->scan_tmp.p, st);
     u32 tail[2];
     CK(cudaMemcpyAsync(&tail[0], w.entry_offset + R, 4, cudaMemcpyDeviceToHost, st), "D2H");
+    u32 esc1 = 0;
     CK(cudaMemcpyAsync(&tail[1], w.counters + 4, 4, cudaMemcpyDeviceToHost, st), "D2H");
+    CK(cudaMemcpyAsync(&esc1, w.counters + 10, 4, cudaMemcpyDeviceToHost, st), "D2H");
     CK(cudaStreamSynchronize(st), "covariates");
     const u64 N = tail[0];
     CK(eng->entries.ensure(al(N * 8 + 8)), "entries");
@@ -505,7 +528,7 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
     eng->stats.total_reads += R;
     eng->stats.filtered_reads += cnt[5];
     eng->stats.baq_reads += cnt[6];
-    eng->stats.baq_fp64_escalated_reads += tail[1];
+    eng->stats.baq_fp64_escalated_reads += u64(tail[1]) + esc1;
     eng->stats.num_batches++;
     eng->last_R = R;
     eng->last_Q = Q;
@@ -523,6 +546,8 @@ fp_status fp_engine_finalize(fp_engine *eng) {
     cudaEventRecord(eng->ev[7], st);
     const KeySpace ks = eng->tables.ks;
     const u32 T = ks.total;
+    launch_merge_stage(eng->tables, st);
+    eng->staged_bases = 0;
     DevBuf flags, pos, rows, rkey, robs, rmism, rexp, rest, rcoef, remp, rg, tmp;
     auto cleanup = [&]() {
         DevBuf *bs[] = {&flags, &pos, &rows, &rkey, &robs, &rmism, &rexp, &rest, &rcoef, &remp, &rg, &tmp};
@@ -684,6 +709,8 @@ fp_status fp_engine_reset(fp_engine *eng) {
     const size_t n = eng->tables.ks.total;
     CK(cudaMemsetAsync(eng->tab_obs.p, 0, n * sizeof(unsigned long long), eng->st), "reset");
     CK(cudaMemsetAsync(eng->tab_mism.p, 0, n * sizeof(float), eng->st), "reset");
+    CK(cudaMemsetAsync(eng->tab_stage.p, 0, n * sizeof(u32), eng->st), "reset");
+    eng->staged_bases = 0;
     CK(cudaStreamSynchronize(eng->st), "reset");
     for (auto &t : eng->out) t = HostTable();
     eng->finalized = false;

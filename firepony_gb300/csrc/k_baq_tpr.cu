@@ -1,0 +1,440 @@
+// K2: the banded glocal BAQ HMM (device/baq.cu:214-697), one thread per read with the band row held in
+// registers. W = 2*BW+1 band slots are fully unrolled, so every cell of a row is a named register: the
+// M/I recurrences from the previous row are register reads, the D chain along the row is the natural
+// sequential recurrence, and rows are updated in place. The forward rows (M, I) needed by MAP go to a
+// per-warp scratch slot, interleaved by lane so each warp store/load moves 32 consecutive words; backward
+// is fused with MAP.
+//
+// Two arithmetic modes share the code:
+//   EXACT (double): the reference's operations in the reference's order, each multiply and add an explicit
+//     __dmul_rn/__dadd_rn (never fused), so every intermediate double equals the reference's host value.
+//     Used for reads the FP32 bound cannot decide.
+//   FP32 (float): fused multiply-adds, with a certified relative error bound. Every HMM value is a sum of
+//     products of non-negative terms, so a computed value is the exact one times (1 + theta) with
+//     |theta| <= (roundings on the deepest path) * 2^-24, and the per-row scalings cancel in the posterior.
+//     Per row a path takes at most 7 roundings (M or I entry: 5 including the emission, 1 for the row
+//     scaling, 1 spare) plus 2 per D step, and a path makes at most refLen D steps, so forward and backward
+//     values carry eps <= (7 qlen + 2 refLen + 8) 2^-24 each and a posterior term eps_z = 2 eps + 2^-24; a
+//     sum of at most 2W terms adds 2W 2^-24, so the ratio (sum of the other terms)/(total) is within
+//     rel = 2 (eps_z + 2W u) + u. A base's MAP quality is undecided when min(q_orig, clamp(floor(t'))) is not
+//     constant for t' within dt = 4.343 rel / (1 - rel) + 1e-4 of the computed t (1e-4 covers logf and the
+//     reference's own double rounding), and its MAP state is undecided when the runner-up term is within
+//     2 eps_z + 2u (relative) of the best. A read whose in-band M
+//     values drop below 1e-30 (where FP32 would start to lose relative precision) is undecided throughout.
+#include "kernels.h"
+
+namespace fpg {
+
+__constant__ double ct_qual2prob[256];
+__constant__ double ct_gap_open;
+
+namespace {
+
+constexpr u32 FULL = 0xffffffffu;
+constexpr int TPR_THREADS = 128;
+
+template <typename T, bool EXACT> struct Ar;
+template <> struct Ar<double, true> {
+    static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+    static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
+    static __device__ __forceinline__ double mad(double a, double b, double c) { return __dadd_rn(__dmul_rn(a, b), c); }
+};
+template <> struct Ar<float, false> {
+    static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
+    static __device__ __forceinline__ float add(float a, float b) { return a + b; }
+    static __device__ __forceinline__ float div(float a, float b) { return a / b; }
+    static __device__ __forceinline__ float mad(float a, float b, float c) { return fmaf(a, b, c); }
+};
+
+__device__ __forceinline__ bool tiny_positive(float v) {
+    // 0 < v < 1e-30 on the bit pattern (v >= 0 here)
+    return (__float_as_uint(v) - 1u) < (0x0DA24260u - 1u);
+}
+__device__ __forceinline__ bool tiny_positive(double) { return false; }
+
+template <typename T>
+__device__ __forceinline__ T emission(const T *em_tab, const T *mis_tab, u8 ref, u8 rd, u8 q) {
+    if (ref == IUPAC_N || rd == IUPAC_N) return T(1);
+    return ref == rd ? em_tab[q] : mis_tab[q];
+}
+
+template <typename T, int W, bool EXACT>
+__global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref, BatchWork w, const u32 *list,
+                                                         const u32 *count, u32 *work_ctr, T *scratch, u32 max_q) {
+    using A = Ar<T, EXACT>;
+    __shared__ T s_em[256], s_mis[256];
+    for (int q = threadIdx.x; q < 256; q += blockDim.x) {
+        const double p = ct_qual2prob[q < MIN_BASE_QUAL ? MIN_BASE_QUAL : q];
+        // calcEpsilon (device/baq.cu:361-372): 1 - p for a match, p * EM for a mismatch
+        s_em[q] = T(1 - p);
+        s_mis[q] = T(p * 0.33333333333);
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const u32 gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    // per-warp scratch: rows 0..max_q, per row W slots x (M, I) then the row's scaling factor; x32 lanes
+    const u64 row_words = u64(W) * 2 + 1;
+    T *slot_base = scratch + u64(gwarp) * (u64(max_q) + 2) * row_words * 32 + lane;
+    auto FS = [&](int row, int s, int st) -> T & { return slot_base[((u64(row) * row_words) + s * 2 + st) * 32]; };
+    auto SC = [&](int row) -> T & { return slot_base[((u64(row) * row_words) + W * 2) * 32]; };
+    const u32 n_list = *count;
+    const T EI = T(0.25);
+    const double GOP = ct_gap_open;
+
+    for (;;) {
+        u32 base = 0;
+        if (lane == 0) base = atomicAdd(work_ctr, 32u);
+        base = __shfl_sync(FULL, base, 0);
+        if (base >= n_list) break;
+        const u32 li = base + lane;
+        if (li >= n_list) continue;
+        const u32 r = list[li];
+
+        // ---- setup (device/baq.cu:247-334) ----
+        const u16 *win = w.win + size_t(r) * 8;
+        const int qx = win[0], qy = win[1];
+        const int hx = w.hmm[size_t(r) * 2], hy = w.hmm[size_t(r) * 2 + 1];
+        const int bw = w.bw[r];
+        int refLen = hy - hx + 1;
+        const int bmLen = refLen;
+        const int qL = qy - qx + 1;
+        const u32 astart = b.astart[r];
+        u64 ref_off;
+        const u32 ahx = hx < 0 ? u32(-hx) : u32(hx);
+        if (hx < 0 && astart < ahx) { ref_off = 0; refLen--; }
+        else ref_off = u64(u32(astart + u32(hx)));
+        const DevContig g = dref.contigs[b.chromosome[r]];
+        const u64 qsym = u64(b.read_start[r]) + qx;
+        const u32 qual0 = b.qual_start[r] + qx;
+        auto REF = [&](int k) -> u8 { return k >= 0 ? contig_at(g, ref_off + u64(k)) : u8(0); };
+        auto QRY = [&](int i) -> u8 { return sym4(b.reads, qsym + u64(i)); };
+        auto QUL = [&](int i) -> u8 { return b.quals[qual0 + i]; };
+
+        const double dsM = 1.0 / (2 * qL + 2);
+        const T sM = T(dsM), sI = sM;
+        const T bM = T((1 - GOP) / bmLen), bI = T(GOP / bmLen);
+        const T m0 = T((1 - GOP - GOP) * (1 - dsM)), m1 = T(GOP * (1 - dsM)), m2 = m1;
+        const T m3 = T((1 - 0.1) * (1 - dsM)), m4 = T(0.1 * (1 - dsM));
+        const T m6 = T(1 - 0.1), m8 = T(0.1);
+        bool under = false;
+
+        T M[W], I[W], D[W];
+        u8 rw[W];  // reference symbol used by slot s in the current row
+#pragma unroll
+        for (int s = 0; s < W; s++) { M[s] = T(0); I[s] = T(0); D[s] = T(0); rw[s] = s >= 1 ? REF(s - 1) : 0; }
+
+        // ---- forward, row 1: k = s, band [1, min(refLen, bw+1)] ----
+        {
+            const u8 q0 = QRY(0), qq0 = QUL(0);
+            const int end = refLen < bw + 1 ? refLen : bw + 1;
+            T sum = T(0);
+#pragma unroll
+            for (int s = 0; s < W; s++) {
+                const bool inb = s >= 1 && s <= end;
+                if (inb) {
+                    const T e = emission<T>(s_em, s_mis, rw[s], q0, qq0);
+                    M[s] = A::mul(e, bM);
+                    I[s] = A::mul(EI, bI);
+                    sum = A::add(sum, A::add(M[s], I[s]));
+                }
+            }
+            SC(1) = sum;
+#pragma unroll
+            for (int s = 0; s < W; s++) {
+                M[s] = A::div(M[s], sum);
+                I[s] = A::div(I[s], sum);
+                FS(1, s, 0) = M[s];
+                FS(1, s, 1) = I[s];
+                if (tiny_positive(M[s])) under = true;
+            }
+        }
+        // ---- forward, rows 2..qL ----
+        // the symbols a row needs are loaded one row ahead so their latency overlaps the previous row
+        u8 nq = qL >= 2 ? QRY(1) : 0, nqq = qL >= 2 ? QUL(1) : 0;
+        u8 nref = REF(W - 1 + (2 - bw > 0 ? 2 - bw : 0) - 1);
+        for (int i = 2; i <= qL; i++) {
+            const u8 qyi = nq, qq = nqq, top = nref;
+            if (i < qL) {
+                nq = QRY(i);
+                nqq = QUL(i);
+                nref = REF(W - 1 + (i + 1 - bw > 0 ? i + 1 - bw : 0) - 1);
+            }
+            const int beg = 1 > i - bw ? 1 : i - bw;
+            const int end = refLen < i + bw ? refLen : i + bw;
+            const int x = i - bw > 0 ? i - bw : 0;  // slot s holds cell k = s + x
+            T sum = T(0);
+            if (i > bw) {
+                // the band slides one cell: slot s now holds k = s + x, whose reference base is REF(s + x - 1)
+#pragma unroll
+                for (int s = 0; s < W - 1; s++) rw[s] = rw[s + 1];
+                rw[W - 1] = top;
+                // M(i,k) reads slot s of row i-1 (cell k-1), I(i,k) reads slot s+1 (cell k): ascending in place
+                T dprev = T(0), mprev = T(0);
+#pragma unroll
+                for (int s = 0; s < W; s++) {
+                    const int k = s + x;
+                    const bool inb = k >= beg && k <= end;
+                    const T oM = M[s], oI = I[s], oD = D[s];
+                    const T nM1 = s + 1 < W ? M[s + 1] : T(0), nI1 = s + 1 < W ? I[s + 1] : T(0);
+                    T m = T(0), ii = T(0), d = T(0);
+                    if (inb) {
+                        const T e = emission<T>(s_em, s_mis, rw[s], qyi, qq);
+                        m = A::mul(e, A::add(A::add(A::mul(m0, oM), A::mul(m3, oI)), A::mul(m6, oD)));
+                        ii = A::mul(EI, A::add(A::mul(m1, nM1), A::mul(m4, nI1)));
+                        d = A::add(A::mul(m2, mprev), A::mul(m8, dprev));
+                        sum = A::add(sum, A::add(A::add(m, ii), d));
+                    }
+                    M[s] = m; I[s] = ii; D[s] = d;
+                    mprev = m; dprev = d;
+                }
+            } else {
+                // growing band (x = 0, slot s = cell k): M(i,k) reads slot s-1, I(i,k) reads slot s
+#pragma unroll
+                for (int s = W - 1; s >= 0; s--) {
+                    const int k = s;
+                    const bool inb = k >= beg && k <= end;
+                    T m = T(0), ii = T(0);
+                    if (inb) {
+                        const T e = emission<T>(s_em, s_mis, rw[s], qyi, qq);
+                        const T pM = s >= 1 ? M[s - 1] : T(0), pI = s >= 1 ? I[s - 1] : T(0),
+                                pD = s >= 1 ? D[s - 1] : T(0);
+                        m = A::mul(e, A::add(A::add(A::mul(m0, pM), A::mul(m3, pI)), A::mul(m6, pD)));
+                        ii = A::mul(EI, A::add(A::mul(m1, M[s]), A::mul(m4, I[s])));
+                    }
+                    M[s] = m; I[s] = ii;
+                }
+                T dprev = T(0), mprev = T(0);
+#pragma unroll
+                for (int s = 0; s < W; s++) {
+                    const int k = s;
+                    const bool inb = k >= beg && k <= end;
+                    T d = T(0);
+                    if (inb) {
+                        d = A::add(A::mul(m2, mprev), A::mul(m8, dprev));
+                        sum = A::add(sum, A::add(A::add(M[s], I[s]), d));
+                    }
+                    D[s] = d;
+                    mprev = M[s]; dprev = d;
+                }
+            }
+            SC(i) = sum;
+            const T inv = A::div(T(1), sum);
+#pragma unroll
+            for (int s = 0; s < W; s++) {
+                M[s] = A::mul(M[s], inv);
+                I[s] = A::mul(I[s], inv);
+                D[s] = A::mul(D[s], inv);
+                FS(i, s, 0) = M[s];
+                FS(i, s, 1) = I[s];
+                if (tiny_positive(M[s])) under = true;
+            }
+        }
+        // s[qL+1]: band cells of row qL (slots 0..2bw with k in [1, refLen])
+        T sLast = T(0);
+        {
+            const int x = qL - bw > 0 ? qL - bw : 0;
+#pragma unroll
+            for (int s = 0; s < W; s++) {
+                const int k = s + x;
+                if (s <= 2 * bw && k >= 1 && k <= refLen) sLast = A::add(sLast, A::add(A::mul(M[s], sM), A::mul(I[s], sI)));
+            }
+        }
+        const T sQ = SC(qL);
+
+        // ---- backward fused with MAP ----
+        // slot s of row i holds cell k = s + x(i); the reference symbol it needs is REF(k)
+        T bMv[W], bIv[W], bDv[W];
+        {
+            const int x = qL - bw > 0 ? qL - bw : 0;
+            const T v = A::div(A::div(sM, sQ), sLast);
+#pragma unroll
+            for (int s = 0; s < W; s++) {
+                const int k = s + x;
+                const bool cell = s <= 2 * bw && k >= 1 && k <= refLen;
+                bMv[s] = cell ? v : T(0);
+                bIv[s] = cell ? v : T(0);
+                bDv[s] = T(0);
+                rw[s] = REF(k);
+            }
+        }
+        // certified FP32 bounds (see the file comment): per-direction eps, posterior term eps_z, sums of up to
+        // 2W terms, ratio excl/total and runner-up test
+        const float u = 5.9604644775390625e-8f;
+        const float eps = float((7.0 * qL + 2.0 * refLen + 8.0) * 5.9604644775390625e-8);
+        const float eps_z = 2.0f * eps + u;
+        const float rel = 2.0f * (eps_z + 2.0f * W * u) + u;
+        const float rel_state = 2.0f * eps_z + 2.0f * u;
+        const float dt = 4.343f * rel / (1.0f - rel) + 1e-4f;
+        for (int i = qL; i >= 1; i--) {
+            const int beg = 1 > i - bw ? 1 : i - bw;
+            const int end = refLen < i + bw ? refLen : i + bw;
+            const int x = i - bw > 0 ? i - bw : 0;
+            // forward row i (for MAP) and this row's inputs are loaded first: the backward arithmetic of the
+            // row runs while the loads are in flight
+            T fM[W], fI[W];
+#pragma unroll
+            for (int s = 0; s < W; s++) {
+                fM[s] = FS(i, s, 0);
+                fI[s] = FS(i, s, 1);
+            }
+            if (i < qL) {
+                const u8 qyi1 = QRY(i), qq1 = QUL(i);
+                const T scale_i = SC(i);
+                const u8 ref0 = REF(x);
+                const T y = (i > 1) ? T(1) : T(0);
+                const bool grow = i < bw;  // row i+1 still in the growing band
+                if (!grow) {
+                    // x(i) = x(i+1) - 1: slots move up one cell; slot 0 takes cell x
+#pragma unroll
+                    for (int s = W - 1; s >= 1; s--) rw[s] = rw[s - 1];
+                    rw[0] = ref0;
+                }
+                // descending in place. B_M(i+1, k+1) is slot s of row i+1 (sliding) or slot s+1 (growing, carried
+                // from the previous iteration); B_I(i+1, k) is slot s-1 (sliding, not yet overwritten) or slot s.
+                T dnext = T(0), carryM = T(0);
+#pragma unroll
+                for (int s = W - 1; s >= 0; s--) {
+                    const int k = s + x;
+                    const bool inb = k >= beg && k <= end;
+                    const T oldM = bMv[s], oldI = bIv[s];
+                    const T nbm = grow ? carryM : oldM;
+                    const T bi1 = grow ? oldI : (s >= 1 ? bIv[s - 1] : T(0));
+                    T bm = T(0), bi = T(0), bd = T(0);
+                    if (inb) {
+                        T e = T(0);
+                        if (k < refLen) e = A::mul(emission<T>(s_em, s_mis, rw[s], qyi1, qq1), nbm);
+                        bm = A::add(A::add(A::mul(e, m0), A::mul(A::mul(EI, m1), bi1)), A::mul(m2, dnext));
+                        bi = A::add(A::mul(e, m3), A::mul(A::mul(EI, m4), bi1));
+                        bd = A::mul(A::add(A::mul(e, m6), A::mul(m8, dnext)), y);
+                    }
+                    bMv[s] = bm; bIv[s] = bi; bDv[s] = bd;
+                    dnext = bd;
+                    carryM = oldM;
+                }
+                const T yy = A::div(T(1), scale_i);
+#pragma unroll
+                for (int s = 0; s < W; s++) {
+                    bMv[s] = A::mul(bMv[s], yy);
+                    bIv[s] = A::mul(bIv[s], yy);
+                    bDv[s] = A::mul(bDv[s], yy);
+                    if (tiny_positive(bMv[s])) under = true;
+                }
+            }
+            // ---- MAP for row i (device/baq.cu:619-681): first maximum in (k, M before I) order ----
+            T sum = T(0), mx = T(0), second = T(0), excl = T(0);
+            int max_k = -1;
+#pragma unroll
+            for (int s = 0; s < W; s++) {
+                const int k = s + x;
+                if (k >= beg && k <= end) {
+#pragma unroll
+                    for (int st = 0; st < 2; st++) {
+                        const T z = A::mul(st == 0 ? fM[s] : fI[s], st == 0 ? bMv[s] : bIv[s]);
+                        sum = A::add(sum, z);
+                        if (z > mx) {
+                            if (!EXACT) { excl = A::add(excl, mx); second = mx; }
+                            mx = z;
+                            max_k = (k - 1) << 2 | st;
+                        } else if (!EXACT) {
+                            excl = A::add(excl, z);
+                            if (z > second) second = z;
+                        }
+                    }
+                }
+            }
+            const u32 qi = qual0 + u32(i - 1);
+            if (EXACT) {
+                const double p = double(A::div(mx, sum));
+                // -4.343 * log(1 - max) + .499 with no fused operation; (int) saturates like the reference's
+                // CUDA build (+inf -> INT_MAX, NaN -> 0)
+                const double t = __dadd_rn(__dmul_rn(-4.343, log(__dsub_rn(1.0, p))), 0.499);
+                const int kq = int(t);
+                w.baq_q[qi] = u8(kq > 100 ? 99 : (kq < MIN_BASE_QUAL ? MIN_BASE_QUAL : kq));
+                w.baq_state[qi] = u32(max_k);
+                w.baq_amb[qi] = 0;
+            } else {
+                const int qo = QUL(i - 1);
+                u8 amb = 0;
+                int qv = MIN_BASE_QUAL;
+                u32 state = U32_NONE;
+                if (!(sum > T(0)) || max_k < 0) {
+                    amb = 3;
+                } else {
+                    state = u32(max_k);
+                    if (float(second) >= float(mx) * (1.0f - rel_state)) amb |= 2;
+                    const float ratio = float(excl) / float(sum);
+                    const float tq = ratio > 0.f ? -4.343f * logf(ratio) + 0.499f : __int_as_float(0x7f800000);
+                    const float lo = tq - dt, hi = tq + dt;
+                    auto capped = [&](float tt) {
+                        int k;
+                        if (!(tt == tt)) k = 0;
+                        else if (tt >= 2147483520.0f) k = 2147483647;
+                        else k = int(floorf(tt));
+                        return k > 100 ? 99 : (k < MIN_BASE_QUAL ? MIN_BASE_QUAL : k);
+                    };
+                    qv = capped(tq);
+                    const int flo = capped(lo), fhi = capped(hi);
+                    if (qo <= 99) {
+                        if ((flo < qo ? flo : qo) != (fhi < qo ? fhi : qo)) amb |= 1;
+                    } else if (!(hi < 100.f && flo == fhi) && !(lo >= 101.5f)) {
+                        amb |= 1;
+                    }
+                }
+                w.baq_q[qi] = u8(qv);
+                w.baq_state[qi] = state;
+                w.baq_amb[qi] = amb;
+            }
+        }
+        if (!EXACT && under) {
+            for (int i = 0; i < qL; i++) w.baq_amb[qual0 + i] = 3;
+        }
+    }
+}
+
+template <typename T, int W, bool EXACT>
+void launch_one(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
+                u32 max_reads, u32 *ctr, T *scratch, u64 scratch_elems, u32 max_q, cudaStream_t s) {
+    const u64 per_warp = (u64(max_q) + 2) * (u64(W) * 2 + 1) * 32;
+    u64 warps = scratch_elems / per_warp;
+    u64 blocks = warps / (TPR_THREADS / 32);
+    const u64 need = (u64(max_reads) + TPR_THREADS - 1) / TPR_THREADS;
+    if (blocks > need) blocks = need;
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    if (blocks == 0) return;
+    cudaMemsetAsync(ctr, 0, sizeof(u32), s);
+    k_baq_tpr<T, W, EXACT><<<u32(blocks), TPR_THREADS, 0, s>>>(b, ref, w, list, count, ctr, scratch, max_q);
+    g_kernel_launches++;
+}
+
+}  // namespace
+
+void baq_tpr_set_constants(const HmmConst &c) {
+    cudaMemcpyToSymbol(ct_qual2prob, c.qual2prob, sizeof(c.qual2prob));
+    cudaMemcpyToSymbol(ct_gap_open, &c.gap_open, sizeof(double));
+}
+
+u64 baq_tpr_scratch_bytes(int band_class, bool exact, u32 max_q) {
+    const int W = band_class == 0 ? 15 : 31;
+    const u64 per_warp = (u64(max_q) + 2) * (u64(W) * 2 + 1) * 32 * (exact ? 8 : 4);
+    return per_warp * (152 * 8) * (TPR_THREADS / 32);
+}
+
+void launch_baq_tpr(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
+                    u32 max_reads, int band_class, bool exact, u32 *ctr, void *scratch, u64 scratch_bytes, u32 max_q,
+                    cudaStream_t s) {
+    if (!max_reads) return;
+    if (exact) {
+        if (band_class == 0)
+            launch_one<double, 15, true>(b, ref, w, list, count, max_reads, ctr, (double *)scratch, scratch_bytes / 8, max_q, s);
+        else
+            launch_one<double, 31, true>(b, ref, w, list, count, max_reads, ctr, (double *)scratch, scratch_bytes / 8, max_q, s);
+    } else {
+        if (band_class == 0)
+            launch_one<float, 15, false>(b, ref, w, list, count, max_reads, ctr, (float *)scratch, scratch_bytes / 4, max_q, s);
+        else
+            launch_one<float, 31, false>(b, ref, w, list, count, max_reads, ctr, (float *)scratch, scratch_bytes / 4, max_q, s);
+    }
+}
+
+}  // namespace fpg

@@ -88,104 +88,255 @@ __device__ __forceinline__ void context_keys(const ReadKeys &k, int off, u32 &cm
     if (num >= 3) ci = ((ctx >> (num - 3) * 2) << 4) | 3;
 }
 
+constexpr int COV_WARPS = 8;
+constexpr u32 FULL = 0xffffffffu;
+
+struct CovSmem {
+    u8 q[512];
+    u8 bf[512];
+    u8 tag[512];
+    u8 sym[512];
+};
+
+__device__ __forceinline__ void context_keys_smem(const u8 *sym, bool neg, us2 hq, int off, u32 &cm, u32 &ci) {
+    cm = CONTEXT_INVALID;
+    ci = CONTEXT_INVALID;
+    const int dir = neg ? 1 : -1;
+    const int avail = neg ? int(hq.y) - off + 1 : off - int(hq.x) + 1;
+    const int nb = avail < 3 ? avail : 3;
+    if (nb < 2) return;
+    u32 ctx = 0;
+    int num = 0;
+    for (int j = 0, i = off; j < nb; j++, i += dir) {
+        const u8 bp = sym[i];
+        if (bp != IUPAC_A && bp != IUPAC_C && bp != IUPAC_T && bp != IUPAC_G) break;
+        ctx = (ctx << 2) | u32(31 - __clz(u32(bp)));
+        num++;
+    }
+    if (neg) ctx = ~ctx & ((1u << (num * 2)) - 1);
+    if (num >= 2) cm = ((ctx >> (num - 2) * 2) << 4) | 2;
+    if (num >= 3) ci = ((ctx >> (num - 3) * 2) << 4) | 3;
+}
+
+// warp-aggregated increment: lanes holding the same key add their count through one atomic
+__device__ __forceinline__ void agg_add(u32 *cnt, u32 key, bool valid, int lane) {
+    const u32 k = valid ? key : 0xFFFFFFFFu;
+    const u32 peers = __match_any_sync(FULL, k);
+    if (valid && (__ffs(peers) - 1) == lane) atomicAdd(&cnt[key], u32(__popc(peers)));
+}
+// adds n to both counters of the aligned (I, D) pair starting at `key` (slot 2) with one 64-bit atomic
+__device__ __forceinline__ void add_pair(u32 *cnt, u32 key, u32 n) {
+    atomicAdd(reinterpret_cast<unsigned long long *>(cnt + key), (unsigned long long)n | ((unsigned long long)n << 32));
+}
+
+// One warp per read. Lanes stage the read's qualities, flags, BQ tags and bases in shared memory, then walk
+// the read's CIGAR events 32 at a time (lane = event).
 template <bool EMIT>
-__global__ void __launch_bounds__(128) k_cov(DevBatch b, BatchWork w, Tables t) {
-    const u32 r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= b.R) return;
-    if (w.status[r] != RS_ACTIVE) {
-        if (!EMIT) w.entry_count[r] = 0;
-        return;
-    }
-    const u16 *win = w.win + size_t(r) * 8;
-    ReadKeys k;
-    k.rg = b.rg[r];
-    k.qs = b.qual_start[r];
-    k.rs = b.read_start[r];
-    const u16 fl = b.flags[r];
-    k.neg = fl & F_REVERSE;
-    k.paired_second = (fl & F_PAIRED) && (fl & F_READ2);
-    k.cw = us2{win[0], win[1]};
-    k.reads = b.reads;
-    const u8 *q = b.quals + k.qs;
-    const u8 *bf = w.bflags + k.qs;
-    const int n = int(k.cw.y) - int(k.cw.x) + 1;
-    float *frac = w.frac + size_t(k.qs) * 3;
-
-    if (!EMIT) {
-        // high-quality window (LOW_QUAL_TAIL = 2)
-        us2 h = k.cw;
-        while (q[h.x] <= 2 && h.x < h.y) h.x++;
-        while (q[h.y] <= 2 && h.y > h.x) h.y--;
-        w.win[size_t(r) * 8 + 6] = h.x;
-        w.win[size_t(r) * 8 + 7] = h.y;
-        k.hq = h;
-        const u8 *tg = w.tag + k.qs + k.cw.x;
-        fractional_errors(bf + k.cw.x, tg, n, BF_SNP, frac + size_t(k.cw.x) * 3 + 0, 3);
-        fractional_errors(bf + k.cw.x, tg, n, BF_INS, frac + size_t(k.cw.x) * 3 + 1, 3);
-        fractional_errors(bf + k.cw.x, tg, n, BF_DEL, frac + size_t(k.cw.x) * 3 + 2, 3);
-    } else {
-        k.hq = us2{win[6], win[7]};
-    }
-
-    const u32 cs = w.cigar_offsets[b.cigar_start[r]];
-    const u32 ce = w.cigar_offsets[b.cigar_start[r] + b.cigar_len[r]];
+__global__ void __launch_bounds__(COV_WARPS * 32) k_cov(DevBatch b, BatchWork w, Tables t) {
+    __shared__ CovSmem smem[COV_WARPS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    CovSmem &sm = smem[warp];
+    const u32 lt = (1u << lane) - 1;
     const KeySpace ks = t.ks;
-    u32 nnz = 0;
-    u64 *out = EMIT ? w.entries + w.entry_offset[r] : nullptr;
-    const u32 rgq = k.rg * Q_SPAN;
-    for (u32 e = cs; e < ce; e++) {
-        const u32 rc = w.ev_rc[e];
-        const u16 off = u16(rc & 0xFFFF);
-        if (off == U16_NONE) continue;
-        if (off < k.cw.x || off > k.cw.y) continue;
-        if (!(bf[off] & BF_ACTIVE)) continue;
-        if (w.ev_type[e] == EV_S) continue;
-        const u32 qm = q[off];
-        const float mm[3] = {frac[size_t(off) * 3 + 0], frac[size_t(off) * 3 + 1], frac[size_t(off) * 3 + 2]};
-        const u32 qv[3] = {qm, 45, 45};
-        u32 sub, ind, cm, ci;
-        cycle_keys(k, off, sub, ind);
-        context_keys(k, off, cm, ci);
-        const u32 cyc[3] = {sub, ind, ind};
-        const u32 ctx[3] = {cm, ci, ci};
-#pragma unroll
-        for (u32 ev = 0; ev < 3; ev++) {
-            const u32 rq = rgq + qv[ev];
-            const u32 kq = ks.qual_base + rq * 3 + ev;
-            const bool vc = cyc[ev] != CYCLE_INVALID;
-            const u32 kc = vc ? ks.cycle_base + (rq * CYCLE_SPAN + cyc[ev]) * 3 + ev : 0;
-            const bool vx = ctx[ev] != CONTEXT_INVALID;
-            const u32 kx = vx ? ks.context_base + (rq * CONTEXT_SPAN + context_rank(ctx[ev])) * 3 + ev : 0;
-            if (!EMIT) {
-                atomicAdd(&t.obs[kq], 1ull);
-                if (vc) atomicAdd(&t.obs[kc], 1ull);
-                if (vx) atomicAdd(&t.obs[kx], 1ull);
+    for (u32 r = blockIdx.x * COV_WARPS + warp; r < b.R; r += gridDim.x * COV_WARPS) {
+        if (w.status[r] != RS_ACTIVE) {
+            if (!EMIT && lane == 0) w.entry_count[r] = 0;
+            continue;
+        }
+        const u16 *win = w.win + size_t(r) * 8;
+        const us2 cw = {win[0], win[1]};
+        const u32 qs = b.qual_start[r], rs = b.read_start[r], rlen = b.read_len[r];
+        const u32 rg = b.rg[r];
+        const u16 fl = b.flags[r];
+        const bool neg = fl & F_REVERSE;
+        const bool second = (fl & F_PAIRED) && (fl & F_READ2);
+        __syncwarp();
+        for (u32 i = lane; i < rlen; i += 32) {
+            sm.q[i] = b.quals[qs + i];
+            sm.bf[i] = w.bflags[qs + i];
+            sm.tag[i] = w.tag[qs + i];
+            sm.sym[i] = sym4(b.reads, u64(rs) + i);
+        }
+        __syncwarp();
+        float *frac = w.frac + size_t(qs) * 3;
+        us2 hq;
+        if (!EMIT) {
+            // high-quality window (device/covariates.cu:215-246): first base in [x, y) with q > 2, else y;
+            // then the last base in (x', y] with q > 2, else x'
+            u32 hx = cw.y;
+            for (u32 c = cw.x; c < cw.y; c += 32) {
+                const u32 pos = c + lane;
+                const u32 m = __ballot_sync(FULL, pos < cw.y && sm.q[pos < 511 ? pos : 0] > 2);
+                if (m) { hx = c + __ffs(m) - 1; break; }
             }
-            if (mm[ev] != 0.0f) {
-                const u64 fb = u64(__float_as_uint(mm[ev]));
-                if (EMIT) {
-                    out[nnz] = (u64(kq) << 32) | fb;
-                    if (vc) out[nnz + 1] = (u64(kc) << 32) | fb;
-                    if (vx) out[nnz + 1 + (vc ? 1 : 0)] = (u64(kx) << 32) | fb;
+            u32 hy = hx;
+            for (int c = int(cw.y); c > int(hx); c -= 32) {
+                const int pos = c - lane;
+                const u32 m = __ballot_sync(FULL, pos > int(hx) && sm.q[pos > 0 ? pos : 0] > 2);
+                if (m) { hy = u32(c - (__ffs(m) - 1)); break; }
+            }
+            hq = us2{u16(hx), u16(hy)};
+            if (lane == 0) {
+                w.win[size_t(r) * 8 + 6] = hq.x;
+                w.win[size_t(r) * 8 + 7] = hq.y;
+            }
+            if (lane < 3) {
+                const u8 bit = lane == 0 ? BF_SNP : (lane == 1 ? BF_INS : BF_DEL);
+                fractional_errors(sm.bf + cw.x, sm.tag + cw.x, int(cw.y) - int(cw.x) + 1, bit,
+                                  frac + size_t(cw.x) * 3 + lane, 3);
+            }
+            __syncwarp();
+        } else {
+            hq = us2{win[6], win[7]};
+        }
+
+        const u32 cs = w.cigar_offsets[b.cigar_start[r]];
+        const u32 ce = w.cigar_offsets[b.cigar_start[r] + b.cigar_len[r]];
+        const u32 rgq = rg * Q_SPAN;
+        const int readLength = int(cw.y) - int(cw.x) + 1;
+        const int order = second ? -1 : 1;
+        u32 gathered_total = 0;
+        u32 nnz_total = 0;
+        u64 *out = EMIT ? w.entries + w.entry_offset[r] : nullptr;
+        for (u32 base = cs; base < ce; base += 32) {
+            const u32 e = base + lane;
+            bool g = false;
+            u16 off = 0;
+            if (e < ce) {
+                const u32 rc = w.ev_rc[e];
+                off = u16(rc & 0xFFFF);
+                g = off != U16_NONE && off >= cw.x && off <= cw.y && (sm.bf[off] & BF_ACTIVE) &&
+                    w.ev_type[e] != EV_S;
+            }
+            const u32 gm = __ballot_sync(FULL, g);
+            if (!gm) continue;
+            gathered_total += __popc(gm);
+            // keys (covariate chains of device/covariates/packer_*.h)
+            u32 qm = 0, sub = 0, ind = CYCLE_INVALID, cm = CONTEXT_INVALID, ci = CONTEXT_INVALID;
+            float mm0 = 0.f, mm1 = 0.f, mm2 = 0.f;
+            if (g) {
+                qm = sm.q[off];
+                const int i = int(off) - int(cw.x);
+                int cycle, inc;
+                if (neg) { cycle = readLength * order; inc = -order; }
+                else { cycle = order; inc = order; }
+                cycle += i * inc;
+                u32 res = u32(cycle < 0 ? -cycle : cycle) << 1;
+                if (cycle < 0) res++;
+                sub = res;
+                ind = (i < 4 || i > readLength - 5) ? CYCLE_INVALID : res;
+                context_keys_smem(sm.sym, neg, hq, off, cm, ci);
+                mm0 = frac[size_t(off) * 3 + 0];
+                mm1 = frac[size_t(off) * 3 + 1];
+                mm2 = frac[size_t(off) * 3 + 2];
+            }
+            const u32 kq0 = ks.qual_base + (rgq + qm) * EV_SLOTS + 0;
+            const u32 kq1 = ks.qual_base + (rgq + 45) * EV_SLOTS + 2;
+            const u32 kq2 = kq1 + 1;
+            const u32 kc0 = ks.cycle_base + ((rgq + qm) * CYCLE_SPAN + sub) * EV_SLOTS + 0;
+            const bool vci = ind != CYCLE_INVALID;
+            const u32 kc1 = vci ? ks.cycle_base + ((rgq + 45) * CYCLE_SPAN + ind) * EV_SLOTS + 2 : 0;
+            const u32 kc2 = kc1 + 1;
+            const bool vxm = cm != CONTEXT_INVALID, vxi = ci != CONTEXT_INVALID;
+            const u32 kx0 = vxm ? ks.context_base + ((rgq + qm) * CONTEXT_SPAN + context_rank(cm)) * EV_SLOTS + 0 : 0;
+            const u32 kx1 = vxi ? ks.context_base + ((rgq + 45) * CONTEXT_SPAN + context_rank(ci)) * EV_SLOTS + 2 : 0;
+            const u32 kx2 = kx1 + 1;
+            if (!EMIT) {
+                agg_add(t.stage, kq0, g, lane);
+                if (g) {
+                    atomicAdd(&t.stage[kc0], 1u);
+                    if (vci) add_pair(t.stage, kc1, 1u);
                 }
-                nnz += 1 + (vc ? 1 : 0) + (vx ? 1 : 0);
+                agg_add(t.stage, kx0, g && vxm, lane);
+                // the I and D context keys of a base share the context value: aggregate once, add the pair
+                {
+                    const u32 k = (g && vxi) ? kx1 : 0xFFFFFFFFu;
+                    const u32 peers = __match_any_sync(FULL, k);
+                    if (g && vxi && (__ffs(peers) - 1) == lane) add_pair(t.stage, kx1, u32(__popc(peers)));
+                }
+            }
+            // entries with a nonzero mismatch value, in slot order M, I, D; per slot quality, cycle, context
+            u32 cnt = 0;
+            if (g) {
+                if (mm0 != 0.f) cnt += 1 + 1 + (vxm ? 1 : 0);
+                if (mm1 != 0.f) cnt += 1 + (vci ? 1 : 0) + (vxi ? 1 : 0);
+                if (mm2 != 0.f) cnt += 1 + (vci ? 1 : 0) + (vxi ? 1 : 0);
+            }
+            u32 x = cnt;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const u32 y = __shfl_up_sync(FULL, x, d);
+                if (lane >= d) x += y;
+            }
+            const u32 chunk_total = __shfl_sync(FULL, x, 31);
+            if (EMIT && cnt) {
+                u64 *o = out + nnz_total + (x - cnt);
+                u32 j = 0;
+                if (mm0 != 0.f) {
+                    const u64 fb = u64(__float_as_uint(mm0));
+                    o[j++] = (u64(kq0) << 32) | fb;
+                    o[j++] = (u64(kc0) << 32) | fb;
+                    if (vxm) o[j++] = (u64(kx0) << 32) | fb;
+                }
+                if (mm1 != 0.f) {
+                    const u64 fb = u64(__float_as_uint(mm1));
+                    o[j++] = (u64(kq1) << 32) | fb;
+                    if (vci) o[j++] = (u64(kc1) << 32) | fb;
+                    if (vxi) o[j++] = (u64(kx1) << 32) | fb;
+                }
+                if (mm2 != 0.f) {
+                    const u64 fb = u64(__float_as_uint(mm2));
+                    o[j++] = (u64(kq2) << 32) | fb;
+                    if (vci) o[j++] = (u64(kc2) << 32) | fb;
+                    if (vxi) o[j++] = (u64(kx2) << 32) | fb;
+                }
+            }
+            nnz_total += chunk_total;
+            (void)lt;
+        }
+        if (!EMIT && lane == 0) {
+            w.entry_count[r] = nnz_total;
+            if (gathered_total) {
+                // every gathered base adds one observation to the read group's I and D quality keys
+                add_pair(t.stage, ks.qual_base + (rgq + 45) * EV_SLOTS + 2, gathered_total);
             }
         }
     }
-    if (!EMIT) w.entry_count[r] = nnz;
+}
+
+
+__global__ void k_merge_stage(u32 *stage, unsigned long long *obs, u32 n) {
+    const u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const u32 v = stage[i];
+    if (v) {
+        obs[i] += v;
+        stage[i] = 0;
+    }
 }
 
 }  // namespace
 
+void launch_merge_stage(const Tables &t, cudaStream_t s) {
+    const u32 n = t.ks.total;
+    k_merge_stage<<<(n + 255) / 256, 256, 0, s>>>(t.stage, t.obs, n);
+    g_kernel_launches++;
+}
+
+
 void launch_cov_count(const DevBatch &b, const BatchWork &w, const Tables &t, cudaStream_t s) {
     if (!b.R) return;
-    k_cov<false><<<(b.R + 127) / 128, 128, 0, s>>>(b, w, t);
+    u32 blocks = (b.R + COV_WARPS - 1) / COV_WARPS;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_cov<false><<<blocks, COV_WARPS * 32, 0, s>>>(b, w, t);
     g_kernel_launches++;
 }
 
 void launch_cov_emit(const DevBatch &b, const BatchWork &w, const Tables &t, cudaStream_t s) {
     if (!b.R) return;
-    k_cov<true><<<(b.R + 127) / 128, 128, 0, s>>>(b, w, t);
+    u32 blocks = (b.R + COV_WARPS - 1) / COV_WARPS;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_cov<true><<<blocks, COV_WARPS * 32, 0, s>>>(b, w, t);
     g_kernel_launches++;
 }
 

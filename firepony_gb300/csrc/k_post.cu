@@ -29,16 +29,18 @@ __global__ void k_gather_rows(const u32 *flags, const u32 *pos, u32 n, u32 *rows
 // reference key and quality of a dense index
 __device__ __host__ inline void dense_to_key(const KeySpace &ks, u32 d, u32 &key, u32 &q) {
     if (d < ks.cycle_base) {
-        const u32 x = d - ks.qual_base, ev = x % 3, rq = x / 3, rg = rq / Q_SPAN;
+        const u32 x = d - ks.qual_base, ev = slot_ev(x % EV_SLOTS), rq = x / EV_SLOTS, rg = rq / Q_SPAN;
         q = rq % Q_SPAN;
         key = (rg << 10) | (q << 2) | ev;
     } else if (d < ks.context_base) {
-        const u32 x = d - ks.cycle_base, ev = x % 3, y = x / 3, cyc = y % CYCLE_SPAN, rq = y / CYCLE_SPAN;
+        const u32 x = d - ks.cycle_base, ev = slot_ev(x % EV_SLOTS), y = x / EV_SLOTS, cyc = y % CYCLE_SPAN;
+        const u32 rq = y / CYCLE_SPAN;
         const u32 rg = rq / Q_SPAN;
         q = rq % Q_SPAN;
         key = (rg << 20) | (q << 12) | (cyc << 2) | ev;
     } else {
-        const u32 x = d - ks.context_base, ev = x % 3, y = x / 3, cr = y % CONTEXT_SPAN, rq = y / CONTEXT_SPAN;
+        const u32 x = d - ks.context_base, ev = slot_ev(x % EV_SLOTS), y = x / EV_SLOTS, cr = y % CONTEXT_SPAN;
+        const u32 rq = y / CONTEXT_SPAN;
         const u32 rg = rq / Q_SPAN;
         q = rq % Q_SPAN;
         key = (rg << 21) | (q << 13) | (context_value(cr) << 2) | ev;
@@ -74,7 +76,7 @@ __global__ void k_rg_fold(KeySpace ks, const unsigned long long *obs, const floa
     double m = 0.0, e = 0.0;
     bool first = true;
     for (u32 q = 0; q < Q_SPAN; q++) {
-        const u32 d = ks.qual_base + (rg * Q_SPAN + q) * 3 + ev;
+        const u32 d = ks.qual_base + (rg * Q_SPAN + q) * EV_SLOTS + ev_slot(ev);
         const u64 oq = obs[d];
         if (!oq) continue;
         const double mq = double(mism[d]);

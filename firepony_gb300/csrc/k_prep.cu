@@ -580,122 +580,132 @@ __global__ void __launch_bounds__(128) k_prep(DevBatch b, DevRef ref, BatchWork 
 }
 
 // ---------------------------------------------------------------------------------------------------
-// cap_baq_qualities + recode_baq_qualities (device/baq.cu:870-1081) for one BAQ read. In FP32 mode
-// (exact == 0) the HMM outputs can be undecided (baq_amb); if the cap depends on an undecided value the
-// read goes to the escalation list and nothing is written.
-__global__ void __launch_bounds__(128) k_cap(DevBatch b, BatchWork w, const u32 *list, const u32 *count, int exact) {
-    const u32 idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= *count) return;
-    const u32 r = list[idx];
-    const u32 cs = w.cigar_offsets[b.cigar_start[r]];
-    const u32 ce = w.cigar_offsets[b.cigar_start[r] + b.cigar_len[r]];
-    const u32 n = ce - cs;
-    const u32 *rc = w.ev_rc + cs;
-    const u8 *ty = w.ev_type + cs;
-    const u16 *win = w.win + size_t(r) * 8;
-    const us2 wcl = {win[0], win[1]}, rw = {win[4], win[5]};
-    const ss2 hw = {w.hmm[size_t(r) * 2], w.hmm[size_t(r) * 2 + 1]};
-    const u32 qs = b.qual_start[r];
-    const u32 astart = b.astart[r];
-
-    u32 baq_start = 0;
-    for (u32 i = 0; i < n; i++) {
-        const u16 rb = u16(rc[i] & 0xFFFF);
-        if (rb != U16_NONE && rb >= wcl.x) { baq_start = i; break; }
-    }
-    i16 reference_shift = 0, read_shift = 0;
-    if (hw.x < 0 && astart < baq_abs(hw.x)) {
-        reference_shift = i16(baq_abs(hw.x));
-        read_shift = i16(astart);
-    }
-    const i16 refOffset = i16(int(hw.x) - int(rw.x) + int(reference_shift));
-
-    // pass 1: cap_baq<false> — count read bases; pass 2: cap_baq<true> (or decide escalation)
-    u32 readI = 0;
-    for (u32 i = baq_start; i < n; i++) {
-        const u16 rb = u16(rc[i] & 0xFFFF);
-        if (rb != U16_NONE) {
-            if (rb < wcl.x) continue;
-            if (rb > wcl.y) break;
+// cap_baq_qualities + recode_baq_qualities (device/baq.cu:870-1081), one warp per BAQ read. The reference
+// walks the read's events from the first one inside the clipped window (baq_start) to the first one past it,
+// counting reference steps (S, D, M), deletions and read steps (I, M); read coordinates increase along the
+// events, so that walk is a contiguous range and the running counts are prefix counts (ballots).
+// cap_baq<false> is the read-step total check; cap_baq<true> writes min(bq, baq) or 4 per M base and the
+// original quality per I base. In FP32 mode (exact == 0) the HMM outputs can be undecided (baq_amb); if a
+// capped value depends on one, the read goes to the escalation list and nothing is written.
+__global__ void __launch_bounds__(256) k_cap(DevBatch b, BatchWork w, const u32 *list, const u32 *count, int exact) {
+    constexpr u32 FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const u32 lt = (1u << lane) - 1;
+    const u32 nwarps = (gridDim.x * blockDim.x) >> 5;
+    const u32 n_list = *count;
+    for (u32 idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; idx < n_list; idx += nwarps) {
+        const u32 r = list[idx];
+        const u32 cs = w.cigar_offsets[b.cigar_start[r]];
+        const u32 ce = w.cigar_offsets[b.cigar_start[r] + b.cigar_len[r]];
+        const u32 n = ce - cs;
+        const u32 *rc = w.ev_rc + cs;
+        const u8 *ty = w.ev_type + cs;
+        const u16 *win = w.win + size_t(r) * 8;
+        const us2 wcl = {win[0], win[1]}, rw = {win[4], win[5]};
+        const ss2 hw = {w.hmm[size_t(r) * 2], w.hmm[size_t(r) * 2 + 1]};
+        const u32 qs = b.qual_start[r];
+        const u32 astart = b.astart[r];
+        i16 reference_shift = 0, read_shift = 0;
+        if (hw.x < 0 && astart < baq_abs(hw.x)) {
+            reference_shift = i16(baq_abs(hw.x));
+            read_shift = i16(astart);
         }
-        const u8 t = ty[i];
-        if (t == EV_I || t == EV_M) readI++;
-    }
-    const bool need_update = readI == u32(wcl.y - wcl.x + 1);
+        const i16 refOffset = i16(int(hw.x) - int(rw.x) + int(reference_shift));
 
-    if (need_update) {
-        if (!exact) {
-            // does any capped value depend on an undecided HMM output?
-            u32 refI = 0, numD = 0;
-            readI = 0;
-            bool escalate = false;
-            for (u32 i = baq_start; i < n && !escalate; i++) {
+        // baq_start: first event with a read coordinate >= window.x; end: first later event past window.y
+        u32 baq_start = 0;
+        for (u32 c = 0; c < n; c += 32) {
+            const u32 i = c + lane;
+            const u16 rb = i < n ? u16(rc[i] & 0xFFFF) : U16_NONE;
+            const u32 m = __ballot_sync(FULL, rb != U16_NONE && rb >= wcl.x);
+            if (m) { baq_start = c + __ffs(m) - 1; break; }
+        }
+        u32 end = n;
+        for (u32 c = baq_start; c < n; c += 32) {
+            const u32 i = c + lane;
+            const u16 rb = i < n ? u16(rc[i] & 0xFFFF) : U16_NONE;
+            const u32 m = __ballot_sync(FULL, rb != U16_NONE && rb > wcl.y);
+            if (m) { end = c + __ffs(m) - 1; break; }
+        }
+
+        // pass 1: read-step total (cap_baq<false>) and, in FP32 mode, whether any capped value is undecided
+        u32 readI_total = 0, refI_c = 0, numD_c = 0, readI_c = 0;
+        bool escalate = false;
+        for (u32 c = baq_start; c < end; c += 32) {
+            const u32 i = c + lane;
+            const bool in = i < end;
+            const u8 t = in ? ty[i] : EV_S;
+            const bool isM = in && t == EV_M, isI = in && t == EV_I, isD = in && t == EV_D;
+            const bool isRef = in && (t == EV_S || t == EV_D || t == EV_M);
+            const u32 mRef = __ballot_sync(FULL, isRef), mD = __ballot_sync(FULL, isD);
+            const u32 mRead = __ballot_sync(FULL, isM || isI);
+            if (!exact && isM) {
+                const u32 refI = refI_c + __popc(mRef & lt), numD = numD_c + __popc(mD & lt);
+                const u32 readI = readI_c + __popc(mRead & lt);
                 const u16 rb = u16(rc[i] & 0xFFFF);
-                if (rb != U16_NONE) {
-                    if (rb < wcl.x) continue;
-                    if (rb > wcl.y) break;
-                }
-                switch (ty[i]) {
-                case EV_S: refI++; break;
-                case EV_I: readI++; break;
-                case EV_D: refI++; numD++; break;
-                case EV_M: {
-                    const u8 amb = w.baq_amb[qs + rb];
-                    if (amb & 2) {
-                        escalate = true;
-                    } else {
-                        const u32 expectedPos = refI - u32(int(refOffset)) + (i - numD - baq_start - readI) + u32(int(read_shift));
-                        const u32 state = w.baq_state[qs + rb];
-                        const bool decided_min = ((state & 3) != 0) || ((state >> 2) != expectedPos);
-                        if (!decided_min && (amb & 1)) escalate = true;
-                    }
-                    readI++;
-                    refI++;
-                    break;
-                }
+                const u8 amb = w.baq_amb[qs + rb];
+                if (amb & 2) {
+                    escalate = true;
+                } else if (amb & 1) {
+                    const u32 expectedPos = refI - u32(int(refOffset)) + (i - numD - baq_start - readI) + u32(int(read_shift));
+                    const u32 state = w.baq_state[qs + rb];
+                    if (!(((state & 3) != 0) || ((state >> 2) != expectedPos))) escalate = true;
                 }
             }
-            if (escalate) {
-                const u32 slot = atomicAdd(&w.counters[4], 1u);
-                w.esc_list[slot] = r;
-                return;
-            }
+            refI_c += __popc(mRef);
+            numD_c += __popc(mD);
+            readI_c += __popc(mRead);
         }
-        u32 refI = 0, numD = 0;
-        readI = 0;
-        for (u32 i = baq_start; i < n; i++) {
-            const u16 rb = u16(rc[i] & 0xFFFF);
-            if (rb != U16_NONE) {
-                if (rb < wcl.x) continue;
-                if (rb > wcl.y) break;
+        readI_total = readI_c;
+        const bool need_update = readI_total == u32(wcl.y - wcl.x + 1);
+        if (need_update && !exact && __any_sync(FULL, escalate)) {
+            if (lane == 0) {
+                // escalation lists by band class: class 0 (band <= 7) and class 1 (band <= 15)
+                const u32 cls = w.bw[r] <= 7 ? 0 : 1;
+                const u32 slot = atomicAdd(&w.counters[cls ? 10 : 4], 1u);
+                w.esc_list[size_t(cls) * b.R + slot] = r;
             }
-            switch (ty[i]) {
-            case EV_S: refI++; break;
-            case EV_I: w.tag[qs + rb] = b.quals[qs + rb]; readI++; break;
-            case EV_D: refI++; numD++; break;
-            case EV_M: {
-                const u32 expectedPos = refI - u32(int(refOffset)) + (i - numD - baq_start - readI) + u32(int(read_shift));
-                const u8 oq = b.quals[qs + rb];
-                const u8 bq = w.baq_q[qs + rb];
-                const u32 state = w.baq_state[qs + rb];
-                const bool isIndel = (state & 3) != 0;
-                const u32 pos = state >> 2;
-                w.tag[qs + rb] = (isIndel || pos != expectedPos) ? u8(MIN_BASE_QUAL) : (bq < oq ? bq : oq);
-                readI++;
-                refI++;
-                break;
-            }
-            }
+            continue;
         }
-    } else {
-        for (u32 i = wcl.x; i <= wcl.y; i++) w.tag[qs + i] = b.quals[qs + i];
-    }
-    // recode_baq_qualities (device/baq.cu:1058-1081)
-    const u32 ql = b.qual_len[r];
-    for (u32 i = 0; i < ql; i++) {
-        const u8 v = w.tag[qs + i];
-        if (v == 0xFF) continue;
-        w.tag[qs + i] = u8(u8(b.quals[qs + i] + 64) - v);
+        if (need_update) {
+            refI_c = numD_c = readI_c = 0;
+            for (u32 c = baq_start; c < end; c += 32) {
+                const u32 i = c + lane;
+                const bool in = i < end;
+                const u8 t = in ? ty[i] : EV_S;
+                const bool isM = in && t == EV_M, isI = in && t == EV_I, isD = in && t == EV_D;
+                const bool isRef = in && (t == EV_S || t == EV_D || t == EV_M);
+                const u32 mRef = __ballot_sync(FULL, isRef), mD = __ballot_sync(FULL, isD);
+                const u32 mRead = __ballot_sync(FULL, isM || isI);
+                if (isI) {
+                    const u16 rb = u16(rc[i] & 0xFFFF);
+                    w.tag[qs + rb] = b.quals[qs + rb];
+                } else if (isM) {
+                    const u32 refI = refI_c + __popc(mRef & lt), numD = numD_c + __popc(mD & lt);
+                    const u32 readI = readI_c + __popc(mRead & lt);
+                    const u16 rb = u16(rc[i] & 0xFFFF);
+                    const u32 expectedPos = refI - u32(int(refOffset)) + (i - numD - baq_start - readI) + u32(int(read_shift));
+                    const u8 oq = b.quals[qs + rb];
+                    const u8 bq = w.baq_q[qs + rb];
+                    const u32 state = w.baq_state[qs + rb];
+                    const bool isIndel = (state & 3) != 0;
+                    w.tag[qs + rb] = (isIndel || (state >> 2) != expectedPos) ? u8(MIN_BASE_QUAL) : (bq < oq ? bq : oq);
+                }
+                refI_c += __popc(mRef);
+                numD_c += __popc(mD);
+                readI_c += __popc(mRead);
+            }
+        } else {
+            for (u32 i = wcl.x + lane; i <= wcl.y; i += 32) w.tag[qs + i] = b.quals[qs + i];
+        }
+        __syncwarp();
+        // recode_baq_qualities (device/baq.cu:1058-1081)
+        const u32 ql = b.qual_len[r];
+        for (u32 i = lane; i < ql; i += 32) {
+            const u8 v = w.tag[qs + i];
+            if (v == 0xFF) continue;
+            w.tag[qs + i] = u8(u8(b.quals[qs + i] + 64) - v);
+        }
     }
 }
 
@@ -722,7 +732,9 @@ void launch_prep(const DevBatch &b, const DevRef &ref, const BatchWork &w, cudaS
 void launch_cap(const DevBatch &b, const BatchWork &w, const u32 *list, const u32 *count, int exact, cudaStream_t s,
                 u32 max_reads) {
     if (!max_reads) return;
-    k_cap<<<(max_reads + 127) / 128, 128, 0, s>>>(b, w, list, count, exact);
+    u32 blocks = (max_reads + 7) / 8;  // one warp per read, 8 warps per block
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_cap<<<blocks, 256, 0, s>>>(b, w, list, count, exact);
     g_kernel_launches++;
 }
 

@@ -27,7 +27,9 @@ struct BatchWork {
     float *frac;             // 3 x float per base (snp, ins, del fractional errors as stored in the table)
     // work lists
     u32 *baq_list;           // reads that need BAQ, by band class
-    u32 *counters;           // [0..3] list sizes per class, [4] escalated count, [5] filtered, [6] baq reads
+    u32 *counters;           // [0..2] list sizes per band class, [4]/[10] escalated reads of class 0/1,
+                             // [5] filtered, [6] BAQ reads, [7] longest BAQ query, [8..9],[11] work counters,
+                             // [12..14] widest band per class
     u32 *esc_list;
     // covariate entries
     u32 *entry_count;        // per read + 1
@@ -43,9 +45,11 @@ struct BatchWork {
 
 struct Tables {
     KeySpace ks;
-    unsigned long long *obs;  // per dense key
+    unsigned long long *obs;  // per dense key: observations (merged from stage)
+    u32 *stage;               // per dense key: observations since the last merge
     float *mism;              // per dense key
 };
+void launch_merge_stage(const Tables &t, cudaStream_t s);
 
 // HMM constants computed on the host with the platform libm (exactly the reference's host values)
 struct HmmConst {
@@ -72,6 +76,12 @@ void baq32_set_constants(const HmmConst &c);
 void launch_baq32(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
                   u32 max_reads, int group_lanes, float *scratch, u32 max_qlen, cudaStream_t s);
 u64 baq32_scratch_floats(int group_lanes, u32 max_qlen);
+
+// k_baq_tpr.cu (thread per read, band in registers; FP32 certified or exact FP64)
+void baq_tpr_set_constants(const HmmConst &c);
+void launch_baq_tpr(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
+                    u32 max_reads, int band_class, bool exact, u32 *ctr, void *scratch, u64 scratch_bytes, u32 max_q,
+                    cudaStream_t s);
 
 // k_covariates.cu
 void launch_cov_count(const DevBatch &b, const BatchWork &w, const Tables &t, cudaStream_t s);
