@@ -39,7 +39,11 @@ class FpTableView(C.Structure):
 class FpStats(C.Structure):
     _fields_ = [("total_reads", C.c_uint64), ("filtered_reads", C.c_uint64), ("baq_reads", C.c_uint64),
                 ("num_batches", C.c_uint64), ("baq_fp64_escalated_reads", C.c_uint64),
-                ("gpu_kernel_launches", C.c_uint64), ("gpu_ms_per_stage", C.c_double * 8)]
+                ("gpu_kernel_launches", C.c_uint64), ("gpu_ms_per_stage", C.c_double * 8),
+                ("baq_reads_by_band", C.c_uint64 * 3), ("baq_escalated_by_band", C.c_uint64 * 2),
+                ("baq_escalated_by_cause", C.c_uint64 * 2),
+                ("baq_band_cells", C.c_uint64 * 3), ("baq_main_launches", C.c_uint64),
+                ("baq_main_ms", C.c_double)]
 
 
 def table_to_numpy(tv: FpTableView) -> dict:

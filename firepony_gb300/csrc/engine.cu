@@ -112,7 +112,7 @@ struct fp_engine {
     // statistics
     fp_stats stats{};
     unsigned long long launch_base = 0;
-    cudaEvent_t ev[10]{};
+    cudaEvent_t ev[12]{};  // [0..8] stage boundaries, [10..11] the band-class-0 BAQ launch
     HmmConst hmm{};
     double qual2err[256];
 
@@ -453,9 +453,12 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
         return FP_OK;
     };
     fp_status s;
+    bool timed_main = false;
     if (eng->baq_mode == FP_BAQ_FP64) {
         for (int c = 0; c < 3; c++) {
+            if (c == 0 && n_cls[0]) { cudaEventRecord(eng->ev[10], st); }
             if ((s = run_fp64(w.baq_list + size_t(c) * R, w.counters + c, n_cls[c], bw_max[c])) != FP_OK) return s;
+            if (c == 0 && n_cls[0]) { cudaEventRecord(eng->ev[11], st); timed_main = true; }
         }
     } else {
         // FP32 with certified bounds (band classes 0 and 1), exact FP64 replay of the undecided reads, and the
@@ -464,8 +467,10 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
         CK(eng->s32.ensure(budget), "BAQ scratch");
         for (int c = 0; c < 2; c++) {
             if (!n_cls[c]) continue;
+            if (c == 0) cudaEventRecord(eng->ev[10], st);
             launch_baq_tpr(b, eng->ref, w, w.baq_list + size_t(c) * R, w.counters + c, n_cls[c], c, false,
                            w.counters + 8 + c, eng->s32.p, budget, max_q, st);
+            if (c == 0) { cudaEventRecord(eng->ev[11], st); timed_main = true; }
             launch_cap(b, w, w.baq_list + size_t(c) * R, w.counters + c, 0, st, n_cls[c]);
         }
         for (int c = 0; c < 2; c++) {
@@ -513,6 +518,10 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
     launch_fold(sorted, N, eng->tables.mism, eng->sort_tmp.p, st);
     cudaEventRecord(eng->ev[6], st);
     u32 dev_err = 0;
+    unsigned long long cells[3] = {0, 0, 0};
+    u32 cause[2] = {0, 0};
+    CK(cudaMemcpyAsync(cells, w.counters + 16, sizeof(cells), cudaMemcpyDeviceToHost, st), "D2H");
+    CK(cudaMemcpyAsync(cause, w.counters + 22, sizeof(cause), cudaMemcpyDeviceToHost, st), "D2H");
     CK(cudaMemcpyAsync(cnt, w.counters, sizeof(cnt), cudaMemcpyDeviceToHost, st), "D2H");
     CK(cudaMemcpyAsync(&dev_err, w.err, 4, cudaMemcpyDeviceToHost, st), "D2H");
     CK(cudaStreamSynchronize(st), "batch");
@@ -529,6 +538,18 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
     eng->stats.filtered_reads += cnt[5];
     eng->stats.baq_reads += cnt[6];
     eng->stats.baq_fp64_escalated_reads += u64(tail[1]) + esc1;
+    for (int c = 0; c < 3; c++) {
+        eng->stats.baq_reads_by_band[c] += n_cls[c];
+        eng->stats.baq_band_cells[c] += cells[c];
+    }
+    eng->stats.baq_escalated_by_cause[0] += cause[0];
+    eng->stats.baq_escalated_by_cause[1] += cause[1];
+    eng->stats.baq_escalated_by_band[0] += tail[1];
+    eng->stats.baq_escalated_by_band[1] += esc1;
+    if (timed_main && cudaEventElapsedTime(&ms, eng->ev[10], eng->ev[11]) == cudaSuccess) {
+        eng->stats.baq_main_ms += ms;
+        eng->stats.baq_main_launches++;
+    }
     eng->stats.num_batches++;
     eng->last_R = R;
     eng->last_Q = Q;

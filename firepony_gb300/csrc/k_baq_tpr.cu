@@ -59,6 +59,19 @@ __device__ __forceinline__ T emission(const T *em_tab, const T *mis_tab, u8 ref,
     return ref == rd ? em_tab[q] : mis_tab[q];
 }
 
+// calcEpsilon for one query base against any reference symbol: the match and mismatch values of the row,
+// with a query N giving 1 for both; a reference N gives 1 (row_emission)
+template <typename T>
+__device__ __forceinline__ void row_emission(const T *em_tab, const T *mis_tab, u8 rd, u8 q, T &e_match, T &e_mis) {
+    const bool n = rd == IUPAC_N;
+    e_match = n ? T(1) : em_tab[q];
+    e_mis = n ? T(1) : mis_tab[q];
+}
+template <typename T>
+__device__ __forceinline__ T cell_emission(u8 ref, u8 rd, T e_match, T e_mis) {
+    return ref == rd ? e_match : (ref == IUPAC_N ? T(1) : e_mis);
+}
+
 template <typename T, int W, bool EXACT>
 __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref, BatchWork w, const u32 *list,
                                                          const u32 *count, u32 *work_ctr, T *scratch, u32 max_q) {
@@ -118,6 +131,9 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
         const T m3 = T((1 - 0.1) * (1 - dsM)), m4 = T(0.1 * (1 - dsM));
         const T m6 = T(1 - 0.1), m8 = T(0.1);
         bool under = false;
+        // interior rows (every slot in the band, no cell at the reference end) take the branch-free path
+        const bool full = 2 * bw + 1 == W;
+        const T EIm1 = A::mul(EI, m1), EIm4 = A::mul(EI, m4);
 
         T M[W], I[W], D[W];
         u8 rw[W];  // reference symbol used by slot s in the current row
@@ -164,7 +180,26 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
             const int end = refLen < i + bw ? refLen : i + bw;
             const int x = i - bw > 0 ? i - bw : 0;  // slot s holds cell k = s + x
             T sum = T(0);
-            if (i > bw) {
+            if (full && i > bw && i + bw < refLen) {
+#pragma unroll
+                for (int s = 0; s < W - 1; s++) rw[s] = rw[s + 1];
+                rw[W - 1] = top;
+                T eq, ex;
+                row_emission<T>(s_em, s_mis, qyi, qq, eq, ex);
+                T dprev = T(0), mprev = T(0);
+#pragma unroll
+                for (int s = 0; s < W; s++) {
+                    const T oM = M[s], oI = I[s], oD = D[s];
+                    const T nM1 = s + 1 < W ? M[s + 1] : T(0), nI1 = s + 1 < W ? I[s + 1] : T(0);
+                    const T e = cell_emission<T>(rw[s], qyi, eq, ex);
+                    const T m = A::mul(e, A::add(A::add(A::mul(m0, oM), A::mul(m3, oI)), A::mul(m6, oD)));
+                    const T ii = A::mul(EI, A::add(A::mul(m1, nM1), A::mul(m4, nI1)));
+                    const T d = A::add(A::mul(m2, mprev), A::mul(m8, dprev));
+                    sum = A::add(sum, A::add(A::add(m, ii), d));
+                    M[s] = m; I[s] = ii; D[s] = d;
+                    mprev = m; dprev = d;
+                }
+            } else if (i > bw) {
                 // the band slides one cell: slot s now holds k = s + x, whose reference base is REF(s + x - 1)
 #pragma unroll
                 for (int s = 0; s < W - 1; s++) rw[s] = rw[s + 1];
@@ -290,6 +325,22 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                     for (int s = W - 1; s >= 1; s--) rw[s] = rw[s - 1];
                     rw[0] = ref0;
                 }
+                if (full && i > bw && i + bw < refLen) {
+                    // interior row below a sliding row: every slot in band and k < refLen
+                    T eq, ex;
+                    row_emission<T>(s_em, s_mis, qyi1, qq1, eq, ex);
+                    T dnext = T(0);
+#pragma unroll
+                    for (int s = W - 1; s >= 0; s--) {
+                        const T bi1 = s >= 1 ? bIv[s - 1] : T(0);
+                        const T e = A::mul(cell_emission<T>(rw[s], qyi1, eq, ex), bMv[s]);
+                        const T bm = A::add(A::add(A::mul(e, m0), A::mul(EIm1, bi1)), A::mul(m2, dnext));
+                        const T bi = A::add(A::mul(e, m3), A::mul(EIm4, bi1));
+                        const T bd = A::mul(A::add(A::mul(e, m6), A::mul(m8, dnext)), y);
+                        bMv[s] = bm; bIv[s] = bi; bDv[s] = bd;
+                        dnext = bd;
+                    }
+                } else {
                 // descending in place. B_M(i+1, k+1) is slot s of row i+1 (sliding) or slot s+1 (growing, carried
                 // from the previous iteration); B_I(i+1, k) is slot s-1 (sliding, not yet overwritten) or slot s.
                 T dnext = T(0), carryM = T(0);
@@ -304,13 +355,14 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                     if (inb) {
                         T e = T(0);
                         if (k < refLen) e = A::mul(emission<T>(s_em, s_mis, rw[s], qyi1, qq1), nbm);
-                        bm = A::add(A::add(A::mul(e, m0), A::mul(A::mul(EI, m1), bi1)), A::mul(m2, dnext));
-                        bi = A::add(A::mul(e, m3), A::mul(A::mul(EI, m4), bi1));
+                        bm = A::add(A::add(A::mul(e, m0), A::mul(EIm1, bi1)), A::mul(m2, dnext));
+                        bi = A::add(A::mul(e, m3), A::mul(EIm4, bi1));
                         bd = A::mul(A::add(A::mul(e, m6), A::mul(m8, dnext)), y);
                     }
                     bMv[s] = bm; bIv[s] = bi; bDv[s] = bd;
                     dnext = bd;
                     carryM = oldM;
+                }
                 }
                 const T yy = A::div(T(1), scale_i);
 #pragma unroll
@@ -324,6 +376,24 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
             // ---- MAP for row i (device/baq.cu:619-681): first maximum in (k, M before I) order ----
             T sum = T(0), mx = T(0), second = T(0), excl = T(0);
             int max_k = -1;
+            if (!EXACT && full && i > bw && i + bw < refLen) {
+                // the old maximum (or z itself) joins the sum of the other terms: excl += min(z, mx) and the
+                // runner-up is max(second, min(z, mx)); ties keep the first maximum
+                const int k0 = (x - 1) << 2;
+#pragma unroll
+                for (int s = 0; s < W; s++) {
+#pragma unroll
+                    for (int st = 0; st < 2; st++) {
+                        const T z = A::mul(st == 0 ? fM[s] : fI[s], st == 0 ? bMv[s] : bIv[s]);
+                        sum = A::add(sum, z);
+                        const T lo = fminf(z, mx);
+                        excl = A::add(excl, lo);
+                        second = fmaxf(second, lo);
+                        max_k = z > mx ? k0 + (s << 2) + st : max_k;
+                        mx = fmaxf(z, mx);
+                    }
+                }
+            } else {
 #pragma unroll
             for (int s = 0; s < W; s++) {
                 const int k = s + x;
@@ -342,6 +412,7 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                         }
                     }
                 }
+            }
             }
             const u32 qi = qual0 + u32(i - 1);
             if (EXACT) {

@@ -569,6 +569,17 @@ __global__ void __launch_bounds__(128) k_prep(DevBatch b, DevRef ref, BatchWork 
             const u32 cls = bw <= 7 ? 0 : (bw <= 15 ? 1 : 2);
             const u32 slot = atomicAdd(&w.counters[cls], 1u);
             w.baq_list[size_t(cls) * b.R + slot] = r;
+            // band cells of the read's HMM (rows 1..qL, reference positions max(1, i-bw)..min(refLen, i+bw)),
+            // the work unit of the BAQ kernels' throughput figures
+            int refLen = int(hw.y) - int(hw.x) + 1;
+            if (hw.x < 0 && rd.astart < baq_abs(hw.x)) refLen--;
+            const int qL = int(wcl.y) - int(wcl.x) + 1;
+            u64 cells = 0;
+            for (int i = 1; i <= qL; i++) {
+                const int lo = 1 > i - int(bw) ? 1 : i - int(bw), hi = refLen < i + int(bw) ? refLen : i + int(bw);
+                if (hi >= lo) cells += u64(hi - lo + 1);
+            }
+            atomicAdd(reinterpret_cast<unsigned long long *>(w.counters + 16) + cls, (unsigned long long)cells);
             atomicAdd(&w.counters[6], 1u);
             atomicMax(&w.counters[7], u32(wcl.y - wcl.x + 1));
             atomicMax(&w.counters[12 + cls], u32(bw));
@@ -630,7 +641,7 @@ __global__ void __launch_bounds__(256) k_cap(DevBatch b, BatchWork w, const u32 
 
         // pass 1: read-step total (cap_baq<false>) and, in FP32 mode, whether any capped value is undecided
         u32 readI_total = 0, refI_c = 0, numD_c = 0, readI_c = 0;
-        bool escalate = false;
+        bool escalate = false, by_state = false;
         for (u32 c = baq_start; c < end; c += 32) {
             const u32 i = c + lane;
             const bool in = i < end;
@@ -646,6 +657,7 @@ __global__ void __launch_bounds__(256) k_cap(DevBatch b, BatchWork w, const u32 
                 const u8 amb = w.baq_amb[qs + rb];
                 if (amb & 2) {
                     escalate = true;
+                    by_state = true;
                 } else if (amb & 1) {
                     const u32 expectedPos = refI - u32(int(refOffset)) + (i - numD - baq_start - readI) + u32(int(read_shift));
                     const u32 state = w.baq_state[qs + rb];
@@ -665,6 +677,9 @@ __global__ void __launch_bounds__(256) k_cap(DevBatch b, BatchWork w, const u32 
                 const u32 slot = atomicAdd(&w.counters[cls ? 10 : 4], 1u);
                 w.esc_list[size_t(cls) * b.R + slot] = r;
             }
+            // escalation cause: some MAP state undecided, or only qualities undecided
+            const bool st = __any_sync(FULL, by_state);
+            if (lane == 0) atomicAdd(&w.counters[st ? 22 : 23], 1u);
             continue;
         }
         if (need_update) {

@@ -185,8 +185,10 @@ class Engine:
     def stats(self) -> dict:
         s = FpStats()
         self._check(lib().fp_engine_get_stats(self.h, C.byref(s)), "get_stats")
-        d = {f: getattr(s, f) for f, _ in FpStats._fields_ if f != "gpu_ms_per_stage"}
-        d["gpu_ms_per_stage"] = list(s.gpu_ms_per_stage)
+        d = {}
+        for f, _ in FpStats._fields_:
+            v = getattr(s, f)
+            d[f] = list(v) if hasattr(v, "__len__") else v
         return d
 
     def debug_last_batch(self, batch) -> dict:

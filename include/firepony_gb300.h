@@ -114,6 +114,13 @@ typedef struct {
     uint64_t baq_fp64_escalated_reads;   /* FP32 mode: reads recomputed in FP64 */
     uint64_t gpu_kernel_launches;        /* kernels launched by this engine since creation */
     double   gpu_ms_per_stage[8];        /* device time per stage (see fp_stage) */
+    uint64_t baq_reads_by_band[3];       /* BAQ reads by band class: bw <= 7, bw <= 15, wider */
+    uint64_t baq_escalated_by_band[2];   /* FP32 mode: FP64 replays of band classes 0 and 1 */
+    uint64_t baq_escalated_by_cause[2];  /* FP32 mode: replays with an undecided MAP state, with undecided
+                                            qualities only */
+    uint64_t baq_band_cells[3];          /* HMM band cells (row x in-band reference positions) per class */
+    uint64_t baq_main_launches;          /* launches of the dominant BAQ kernel (band class 0, FP32 or FP64) */
+    double   baq_main_ms;                /* their device time */
 } fp_stats;
 
 typedef enum {
