@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--baq", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--replay-rpw", type=int, default=0, help="reads per warp of the FP64 replay kernels (0: default)")
     return ap.parse_args()
 
 
@@ -148,7 +149,8 @@ def run_gb300(args, rank, world):
     torch.cuda.set_device(rank)
     K, W = args.steps, args.warmup
     p, ref, batches = make_workload(K, args.batch_reads)
-    eng = Engine(num_read_groups=p.num_read_groups, baq_mode=args.baq, device=rank)
+    eng = Engine(num_read_groups=p.num_read_groups, baq_mode=args.baq, device=rank,
+                 replay_reads_per_warp=args.replay_rpw)
     eng.load_reference(ref)
     stream = torch.cuda.ExternalStream(eng.stream)
 

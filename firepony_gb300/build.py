@@ -29,7 +29,6 @@ ENGINE_UNITS = [
     ("engine.cu", []),
     ("k_prep.cu", []),
     ("k_baq64.cu", ["-fmad=false"]),   # FP64 HMM: bit-exact replay of the reference's operation order
-    ("k_baq32.cu", []),
     ("k_baq_tpr.cu", []),
     ("k_covariates.cu", []),
     ("k_sort.cu", []),

@@ -77,6 +77,7 @@ double gaussian(double value) {  // device/empirical_quality.cu:43-53
 struct fp_engine {
     int device = 0;
     int baq_mode = FP_BAQ_FP32;
+    u32 replay_rpw = 32;  // reads per warp of the FP64 replay kernels
     uint32_t n_rg = 1;
     cudaStream_t st = nullptr;
     std::string err;
@@ -176,9 +177,11 @@ fp_status fp_engine_create(const fp_options *o, fp_engine **out) {
     if (!o || !out) return FP_BAD_INPUT;
     *out = nullptr;
     if (o->num_read_groups == 0 || o->num_read_groups > 256) return FP_BAD_INPUT;
+    if (o->replay_reads_per_warp > 32) return FP_BAD_INPUT;
     fp_engine *eng = new fp_engine();
     eng->device = o->device;
     eng->baq_mode = o->baq_mode;
+    if (o->replay_reads_per_warp) eng->replay_rpw = o->replay_reads_per_warp;
     eng->n_rg = o->num_read_groups;
     cudaError_t e = cudaSetDevice(eng->device);
     if (e != cudaSuccess) {
@@ -198,7 +201,6 @@ fp_status fp_engine_create(const fp_options *o, fp_engine **out) {
     }
     eng->hmm.gap_open = pow(10.0, (-40.0) / 10.);
     baq64_set_constants(eng->hmm);
-    baq32_set_constants(eng->hmm);
     baq_tpr_set_constants(eng->hmm);
     EmpConst ec;
     for (int d = 0; d <= 40; d++) ec.prior[d] = log10(gaussian(double(d)));
@@ -408,7 +410,7 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
         w.bw = reinterpret_cast<u16 *>(p); p += al(R * 2ull);
         w.nerr = reinterpret_cast<u16 *>(p);
     }
-    const size_t pb_bytes = al(Q) * 4 + al(Q * 4) + al(Q * 12);
+    const size_t pb_bytes = al(Q) * 4 + al(Q * 4) + al(Q * 12) + al(Q * 2);
     CK(eng->per_base.ensure(pb_bytes), "per-base arrays");
     {
         char *p = eng->per_base.as<char>();
@@ -417,6 +419,7 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
         w.baq_q = reinterpret_cast<u8 *>(p); p += al(Q);
         w.baq_amb = reinterpret_cast<u8 *>(p); p += al(Q);
         w.baq_state = reinterpret_cast<u32 *>(p); p += al(Q * 4);
+        w.baq_alt = reinterpret_cast<u16 *>(p); p += al(Q * 2);
         w.frac = reinterpret_cast<float *>(p);
     }
     CK(eng->lists.ensure(al(R * 4ull) * 5), "work lists");
@@ -431,6 +434,7 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
 
     // ---- K1 ----
     launch_prep(b, eng->ref, w, st);
+    CK(cudaGetLastError(), "prep launch");
     cudaEventRecord(eng->ev[3], st);
     u32 cnt[16];
     CK(cudaMemcpyAsync(cnt, w.counters, sizeof(cnt), cudaMemcpyDeviceToHost, st), "D2H");
@@ -469,7 +473,7 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
             if (!n_cls[c]) continue;
             if (c == 0) cudaEventRecord(eng->ev[10], st);
             launch_baq_tpr(b, eng->ref, w, w.baq_list + size_t(c) * R, w.counters + c, n_cls[c], c, false,
-                           w.counters + 8 + c, eng->s32.p, budget, max_q, st);
+                           w.counters + 8 + c, eng->s32.p, budget, max_q, 32, st);
             if (c == 0) { cudaEventRecord(eng->ev[11], st); timed_main = true; }
             launch_cap(b, w, w.baq_list + size_t(c) * R, w.counters + c, 0, st, n_cls[c]);
         }
@@ -478,11 +482,12 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
             const u32 *esc = w.esc_list + size_t(c) * R;
             u32 *esc_count = w.counters + (c ? 10 : 4);
             launch_baq_tpr(b, eng->ref, w, esc, esc_count, n_cls[c], c, true, w.counters + 11, eng->s32.p, budget,
-                           max_q, st);
+                           max_q, eng->replay_rpw, st);
             launch_cap(b, w, esc, esc_count, 1, st, n_cls[c]);
         }
         if ((s = run_fp64(w.baq_list + 2ull * R, w.counters + 2, n_cls[2], bw_max[2])) != FP_OK) return s;
     }
+    CK(cudaGetLastError(), "BAQ launch");
     cudaEventRecord(eng->ev[4], st);
 
     // ---- K3 count + scan ----
@@ -508,6 +513,7 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
     w.entries_alt = eng->entries_alt.as<u64>();
     CK(eng->sort_tmp.ensure(std::max(radix_tmp_bytes(N), fold_tmp_bytes(N))), "sort scratch");
     launch_cov_emit(b, w, eng->tables, st);
+    CK(cudaGetLastError(), "covariate launch");
     cudaEventRecord(eng->ev[5], st);
 
     // ---- K4 sort + ordered fold ----
@@ -516,6 +522,7 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
     u64 *sorted = w.entries;
     launch_radix_sort(w.entries, w.entries_alt, N, key_bits, eng->sort_tmp.p, eng->sort_tmp.cap, &sorted, st);
     launch_fold(sorted, N, eng->tables.mism, eng->sort_tmp.p, st);
+    CK(cudaGetLastError(), "sort launch");
     cudaEventRecord(eng->ev[6], st);
     u32 dev_err = 0;
     unsigned long long cells[3] = {0, 0, 0};
@@ -665,6 +672,7 @@ fp_status fp_engine_finalize(fp_engine *eng) {
     std::vector<double> emp(size_t(nrows) + ngr);
     if (nrows + ngr)
         CKF(cudaMemcpyAsync(emp.data(), d_emp, (size_t(nrows) + ngr) * 8, cudaMemcpyDeviceToHost, st), "finalize");
+    CK(cudaGetLastError(), "postprocess launch");
     cudaEventRecord(eng->ev[8], st);
     CKF(cudaStreamSynchronize(st), "finalize");
     gb.release();

@@ -19,8 +19,12 @@
 //     rel = 2 (eps_z + 2W u) + u. A base's MAP quality is undecided when min(q_orig, clamp(floor(t'))) is not
 //     constant for t' within dt = 4.343 rel / (1 - rel) + 1e-4 of the computed t (1e-4 covers logf and the
 //     reference's own double rounding), and its MAP state is undecided when the runner-up term is within
-//     2 eps_z + 2u (relative) of the best. A read whose in-band M
-//     values drop below 1e-30 (where FP32 would start to lose relative precision) is undecided throughout.
+//     2 eps_z + 2u (relative) of the best; such a base also records its rival state when there is exactly
+//     one. Rows are rescaled by powers of two (forward sum 2^64, backward factor 2^32) so that band cells far
+//     from the alignment stay normal numbers; a read with a stored M value below 1e-22 (where a product of the
+//     next row could leave the normal range) is undecided throughout. Posterior terms of such far cells can
+//     still round to subnormals; their absolute error (< 2W 2^-149) is ~1e-70 of the row's total and is
+//     covered by the 2^-24 slack terms above.
 #include "kernels.h"
 
 namespace fpg {
@@ -47,9 +51,16 @@ template <> struct Ar<float, false> {
     static __device__ __forceinline__ float mad(float a, float b, float c) { return fmaf(a, b, c); }
 };
 
+// FP32 row scaling: forward rows are normalised to sum 2^64 (the reference: 1) and backward values carry a
+// factor 2^32, so band cells down to ~1e-41 of their row stay normal numbers. Per-row constants cancel in the
+// MAP ratios; every value, sum and posterior term stays below ~1e34.
+constexpr float FWD_SCALE = 18446744073709551616.0f;    // 2^64
+constexpr float BWD_INIT = 79228162514264337593543950336.0f;  // 2^96 = 2^64 (sLast) x 2^32 (backward factor)
 __device__ __forceinline__ bool tiny_positive(float v) {
-    // 0 < v < 1e-30 on the bit pattern (v >= 0 here)
-    return (__float_as_uint(v) - 1u) < (0x0DA24260u - 1u);
+    // 0 < v < 1e-22 on the bit pattern (v >= 0 here). A stored M value (forward or backward) at or above 1e-22
+    // keeps every product of the next row above 2^-126 (smallest emission 1.7e-10, gap transitions >= 1e-4,
+    // insertion emission 0.25), so no operation of a read without a flag leaves the normal range.
+    return (__float_as_uint(v) - 1u) < (0x1AF1C901u - 1u);
 }
 __device__ __forceinline__ bool tiny_positive(double) { return false; }
 
@@ -74,7 +85,8 @@ __device__ __forceinline__ T cell_emission(u8 ref, u8 rd, T e_match, T e_mis) {
 
 template <typename T, int W, bool EXACT>
 __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref, BatchWork w, const u32 *list,
-                                                         const u32 *count, u32 *work_ctr, T *scratch, u32 max_q) {
+                                                         const u32 *count, u32 *work_ctr, T *scratch, u32 max_q,
+                                                         u32 rpw) {
     using A = Ar<T, EXACT>;
     __shared__ T s_em[256], s_mis[256];
     for (int q = threadIdx.x; q < 256; q += blockDim.x) {
@@ -88,20 +100,23 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
     const u32 gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     // per-warp scratch: rows 0..max_q, per row W slots x (M, I) then the row's scaling factor; x32 lanes
     const u64 row_words = u64(W) * 2 + 1;
-    T *slot_base = scratch + u64(gwarp) * (u64(max_q) + 2) * row_words * 32 + lane;
-    auto FS = [&](int row, int s, int st) -> T & { return slot_base[((u64(row) * row_words) + s * 2 + st) * 32]; };
-    auto SC = [&](int row) -> T & { return slot_base[((u64(row) * row_words) + W * 2) * 32]; };
+    // rpw reads per warp (lanes 0..rpw-1): 32 for the FP32 kernels; the FP64 replays of a few reads spread
+    // them over more warps (their time is the FP64 latency of one read). Scratch is interleaved by rpw.
+    const u32 stride = EXACT ? rpw : 32u;
+    T *slot_base = scratch + u64(gwarp) * (u64(max_q) + 2) * row_words * stride + lane;
+    auto FS = [&](int row, int s, int st) -> T & { return slot_base[((u64(row) * row_words) + s * 2 + st) * stride]; };
+    auto SC = [&](int row) -> T & { return slot_base[((u64(row) * row_words) + W * 2) * stride]; };
     const u32 n_list = *count;
     const T EI = T(0.25);
     const double GOP = ct_gap_open;
 
     for (;;) {
         u32 base = 0;
-        if (lane == 0) base = atomicAdd(work_ctr, 32u);
+        if (lane == 0) base = atomicAdd(work_ctr, EXACT ? rpw : 32u);
         base = __shfl_sync(FULL, base, 0);
         if (base >= n_list) break;
         const u32 li = base + lane;
-        if (li >= n_list) continue;
+        if ((EXACT && u32(lane) >= rpw) || li >= n_list) continue;
         const u32 r = list[li];
 
         // ---- setup (device/baq.cu:247-334) ----
@@ -156,10 +171,17 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                 }
             }
             SC(1) = sum;
+            T inv1 = T(0);
+            if constexpr (!EXACT) inv1 = FWD_SCALE / sum;
 #pragma unroll
             for (int s = 0; s < W; s++) {
-                M[s] = A::div(M[s], sum);
-                I[s] = A::div(I[s], sum);
+                if constexpr (EXACT) {
+                    M[s] = A::div(M[s], sum);
+                    I[s] = A::div(I[s], sum);
+                } else {
+                    M[s] = M[s] * inv1;
+                    I[s] = I[s] * inv1;
+                }
                 FS(1, s, 0) = M[s];
                 FS(1, s, 1) = I[s];
                 if (tiny_positive(M[s])) under = true;
@@ -254,7 +276,7 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                 }
             }
             SC(i) = sum;
-            const T inv = A::div(T(1), sum);
+            const T inv = A::div(EXACT ? T(1) : T(FWD_SCALE), sum);
 #pragma unroll
             for (int s = 0; s < W; s++) {
                 M[s] = A::mul(M[s], inv);
@@ -282,7 +304,13 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
         T bMv[W], bIv[W], bDv[W];
         {
             const int x = qL - bw > 0 ? qL - bw : 0;
-            const T v = A::div(A::div(sM, sQ), sLast);
+            T v;
+            if constexpr (EXACT) {
+                v = A::div(A::div(sM, sQ), sLast);
+            } else {
+                // sM / s(qL) / sLast in reference units, times 2^32: sQ carries 2^64 unless qL == 1, sLast 2^64
+                v = ((sM / sQ) * (qL >= 2 ? FWD_SCALE : 1.0f) / sLast) * BWD_INIT;
+            }
 #pragma unroll
             for (int s = 0; s < W; s++) {
                 const int k = s + x;
@@ -301,12 +329,19 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
         const float rel = 2.0f * (eps_z + 2.0f * W * u) + u;
         const float rel_state = 2.0f * eps_z + 2.0f * u;
         const float dt = 4.343f * rel / (1.0f - rel) + 1e-4f;
+        // the row inputs of the next backward step are loaded one step ahead
+        nq = 0; nqq = 0; nref = 0;
+        if (qL >= 2) {
+            nq = QRY(qL - 1);
+            nqq = QUL(qL - 1);
+            nref = REF(qL - 1 - bw > 0 ? qL - 1 - bw : 0);
+        }
         for (int i = qL; i >= 1; i--) {
             const int beg = 1 > i - bw ? 1 : i - bw;
             const int end = refLen < i + bw ? refLen : i + bw;
             const int x = i - bw > 0 ? i - bw : 0;
-            // forward row i (for MAP) and this row's inputs are loaded first: the backward arithmetic of the
-            // row runs while the loads are in flight
+            // forward row i (for MAP) is loaded first: the backward arithmetic of the row runs while the loads
+            // are in flight
             T fM[W], fI[W];
 #pragma unroll
             for (int s = 0; s < W; s++) {
@@ -314,9 +349,13 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                 fI[s] = FS(i, s, 1);
             }
             if (i < qL) {
-                const u8 qyi1 = QRY(i), qq1 = QUL(i);
+                const u8 qyi1 = nq, qq1 = nqq, ref0 = nref;
+                if (i > 1) {
+                    nq = QRY(i - 1);
+                    nqq = QUL(i - 1);
+                    nref = REF(i - 1 - bw > 0 ? i - 1 - bw : 0);
+                }
                 const T scale_i = SC(i);
-                const u8 ref0 = REF(x);
                 const T y = (i > 1) ? T(1) : T(0);
                 const bool grow = i < bw;  // row i+1 still in the growing band
                 if (!grow) {
@@ -364,13 +403,18 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                     carryM = oldM;
                 }
                 }
-                const T yy = A::div(T(1), scale_i);
+                // 1 / s(i) in reference units: SC(i) carries 2^64 for rows after the first
+                const T yy = A::div(EXACT || i == 1 ? T(1) : T(FWD_SCALE), scale_i);
+                // the cells of column refLen (no emission; they only feed a diagonal neighbour, scaled by their
+                // own tiny value) may decay through the subnormal range: their absolute error (< 2^-149 per
+                // operation) is below 1e-23 of any cell they feed and is not flagged
+                const int last_ok = refLen - 1 - x;
 #pragma unroll
                 for (int s = 0; s < W; s++) {
                     bMv[s] = A::mul(bMv[s], yy);
                     bIv[s] = A::mul(bIv[s], yy);
                     bDv[s] = A::mul(bDv[s], yy);
-                    if (tiny_positive(bMv[s])) under = true;
+                    if (tiny_positive(bMv[s]) && s <= last_ok) under = true;
                 }
             }
             // ---- MAP for row i (device/baq.cu:619-681): first maximum in (k, M before I) order ----
@@ -429,11 +473,36 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                 u8 amb = 0;
                 int qv = MIN_BASE_QUAL;
                 u32 state = U32_NONE;
-                if (!(sum > T(0)) || max_k < 0) {
-                    amb = 3;
+                if (!(sum > T(0)) || !(sum <= T(3.0e38f)) || max_k < 0) {
+                    amb = 7;
                 } else {
                     state = u32(max_k);
-                    if (float(second) >= float(mx) * (1.0f - rel_state)) amb |= 2;
+                    const float thr = float(mx) * (1.0f - rel_state);
+                    if (float(second) >= thr) {
+                        // undecided state: the rivals are the other cells whose term is within the bound of the
+                        // maximum; with exactly one, the capping step can still decide when neither state is the
+                        // match at the base's expected position
+                        amb |= 2;
+                        int rivals = 0;
+                        u32 alt = 0;
+#pragma unroll
+                        for (int s = 0; s < W; s++) {
+                            const int k = s + x;
+                            if (k >= beg && k <= end) {
+#pragma unroll
+                                for (int st = 0; st < 2; st++) {
+                                    const T z = A::mul(st == 0 ? fM[s] : fI[s], st == 0 ? bMv[s] : bIv[s]);
+                                    const u32 idx = u32((k - 1) << 2 | st);
+                                    if (idx != state && float(z) >= thr) {
+                                        if (!rivals) alt = idx;
+                                        rivals++;
+                                    }
+                                }
+                            }
+                        }
+                        if (rivals == 1) w.baq_alt[qi] = u16(alt);
+                        else amb |= 4;
+                    }
                     const float ratio = float(excl) / float(sum);
                     const float tq = ratio > 0.f ? -4.343f * logf(ratio) + 0.499f : __int_as_float(0x7f800000);
                     const float lo = tq - dt, hi = tq + dt;
@@ -458,23 +527,25 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
             }
         }
         if (!EXACT && under) {
-            for (int i = 0; i < qL; i++) w.baq_amb[qual0 + i] = 3;
+            for (int i = 0; i < qL; i++) w.baq_amb[qual0 + i] = 7;
         }
     }
 }
 
 template <typename T, int W, bool EXACT>
 void launch_one(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
-                u32 max_reads, u32 *ctr, T *scratch, u64 scratch_elems, u32 max_q, cudaStream_t s) {
-    const u64 per_warp = (u64(max_q) + 2) * (u64(W) * 2 + 1) * 32;
+                u32 max_reads, u32 *ctr, T *scratch, u64 scratch_elems, u32 max_q, u32 rpw, cudaStream_t s) {
+    const u32 stride = EXACT ? rpw : 32u;
+    const u64 per_warp = (u64(max_q) + 2) * (u64(W) * 2 + 1) * stride;
     u64 warps = scratch_elems / per_warp;
     u64 blocks = warps / (TPR_THREADS / 32);
-    const u64 need = (u64(max_reads) + TPR_THREADS - 1) / TPR_THREADS;
+    const u64 reads_per_block = u64(TPR_THREADS / 32) * (EXACT ? rpw : 32u);
+    const u64 need = (u64(max_reads) + reads_per_block - 1) / reads_per_block;
     if (blocks > need) blocks = need;
     if (blocks > 152 * 8) blocks = 152 * 8;
     if (blocks == 0) return;
     cudaMemsetAsync(ctr, 0, sizeof(u32), s);
-    k_baq_tpr<T, W, EXACT><<<u32(blocks), TPR_THREADS, 0, s>>>(b, ref, w, list, count, ctr, scratch, max_q);
+    k_baq_tpr<T, W, EXACT><<<u32(blocks), TPR_THREADS, 0, s>>>(b, ref, w, list, count, ctr, scratch, max_q, rpw);
     g_kernel_launches++;
 }
 
@@ -493,18 +564,18 @@ u64 baq_tpr_scratch_bytes(int band_class, bool exact, u32 max_q) {
 
 void launch_baq_tpr(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
                     u32 max_reads, int band_class, bool exact, u32 *ctr, void *scratch, u64 scratch_bytes, u32 max_q,
-                    cudaStream_t s) {
+                    u32 rpw, cudaStream_t s) {
     if (!max_reads) return;
     if (exact) {
         if (band_class == 0)
-            launch_one<double, 15, true>(b, ref, w, list, count, max_reads, ctr, (double *)scratch, scratch_bytes / 8, max_q, s);
+            launch_one<double, 15, true>(b, ref, w, list, count, max_reads, ctr, (double *)scratch, scratch_bytes / 8, max_q, rpw, s);
         else
-            launch_one<double, 31, true>(b, ref, w, list, count, max_reads, ctr, (double *)scratch, scratch_bytes / 8, max_q, s);
+            launch_one<double, 31, true>(b, ref, w, list, count, max_reads, ctr, (double *)scratch, scratch_bytes / 8, max_q, rpw, s);
     } else {
         if (band_class == 0)
-            launch_one<float, 15, false>(b, ref, w, list, count, max_reads, ctr, (float *)scratch, scratch_bytes / 4, max_q, s);
+            launch_one<float, 15, false>(b, ref, w, list, count, max_reads, ctr, (float *)scratch, scratch_bytes / 4, max_q, 32u, s);
         else
-            launch_one<float, 31, false>(b, ref, w, list, count, max_reads, ctr, (float *)scratch, scratch_bytes / 4, max_q, s);
+            launch_one<float, 31, false>(b, ref, w, list, count, max_reads, ctr, (float *)scratch, scratch_bytes / 4, max_q, 32u, s);
     }
 }
 

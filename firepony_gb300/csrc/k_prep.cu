@@ -597,7 +597,9 @@ __global__ void __launch_bounds__(128) k_prep(DevBatch b, DevRef ref, BatchWork 
 // events, so that walk is a contiguous range and the running counts are prefix counts (ballots).
 // cap_baq<false> is the read-step total check; cap_baq<true> writes min(bq, baq) or 4 per M base and the
 // original quality per I base. In FP32 mode (exact == 0) the HMM outputs can be undecided (baq_amb); if a
-// capped value depends on one, the read goes to the escalation list and nothing is written.
+// capped value depends on one (an undecided quality of a base whose state is the match at its expected
+// position, or an undecided state whose candidates do not all give MIN_BASE_QUAL), the read goes to the
+// escalation list and nothing is written.
 __global__ void __launch_bounds__(256) k_cap(DevBatch b, BatchWork w, const u32 *list, const u32 *count, int exact) {
     constexpr u32 FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -655,13 +657,26 @@ __global__ void __launch_bounds__(256) k_cap(DevBatch b, BatchWork w, const u32 
                 const u32 readI = readI_c + __popc(mRead & lt);
                 const u16 rb = u16(rc[i] & 0xFFFF);
                 const u8 amb = w.baq_amb[qs + rb];
-                if (amb & 2) {
-                    escalate = true;
-                    by_state = true;
-                } else if (amb & 1) {
+                if (amb) {
                     const u32 expectedPos = refI - u32(int(refOffset)) + (i - numD - baq_start - readI) + u32(int(read_shift));
                     const u32 state = w.baq_state[qs + rb];
-                    if (!(((state & 3) != 0) || ((state >> 2) != expectedPos))) escalate = true;
+                    // the capped value uses the HMM quality only when the MAP state is the match at expectedPos
+                    const bool at_expected = (state & 3) == 0 && (state >> 2) == expectedPos;
+                    if (amb & 4) {
+                        escalate = true;
+                        by_state = true;
+                    } else if (amb & 2) {
+                        // one rival state: decided when neither state is the match at expectedPos (the value is
+                        // MIN_BASE_QUAL whichever wins)
+                        const u32 alt = w.baq_alt[qs + rb];
+                        const bool alt_expected = (alt & 3) == 0 && (alt >> 2) == expectedPos;
+                        if (at_expected || alt_expected) {
+                            escalate = true;
+                            by_state = true;
+                        }
+                    } else if ((amb & 1) && at_expected) {
+                        escalate = true;
+                    }
                 }
             }
             refI_c += __popc(mRef);

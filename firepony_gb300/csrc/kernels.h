@@ -23,7 +23,9 @@ struct BatchWork {
     u8 *tag;                 // BQ tag after recode (0xFF where none)
     u8 *baq_q;               // HMM MAP quality
     u32 *baq_state;          // HMM MAP state
-    u8 *baq_amb;             // FP32 HMM: bit0 quality undecided, bit1 state undecided
+    u8 *baq_amb;             // FP32 HMM: bit0 quality undecided, bit1 state undecided, bit2 more than one
+                             // other state within the bound (or no state at all)
+    u16 *baq_alt;            // FP32 HMM, state undecided with one rival: the rival state
     float *frac;             // 3 x float per base (snp, ins, del fractional errors as stored in the table)
     // work lists
     u32 *baq_list;           // reads that need BAQ, by band class
@@ -72,17 +74,11 @@ void launch_baq64(const DevBatch &b, const DevRef &ref, const BatchWork &w, cons
 u64 baq64_scratch_doubles(u32 threads, u32 max_qlen, u32 max_bw);
 u32 baq64_threads();
 
-// k_baq32.cu
-void baq32_set_constants(const HmmConst &c);
-void launch_baq32(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
-                  u32 max_reads, int group_lanes, float *scratch, u32 max_qlen, cudaStream_t s);
-u64 baq32_scratch_floats(int group_lanes, u32 max_qlen);
-
 // k_baq_tpr.cu (thread per read, band in registers; FP32 certified or exact FP64)
 void baq_tpr_set_constants(const HmmConst &c);
 void launch_baq_tpr(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
                     u32 max_reads, int band_class, bool exact, u32 *ctr, void *scratch, u64 scratch_bytes, u32 max_q,
-                    cudaStream_t s);
+                    u32 reads_per_warp, cudaStream_t s);
 
 // k_covariates.cu
 void launch_cov_count(const DevBatch &b, const BatchWork &w, const Tables &t, cudaStream_t s);

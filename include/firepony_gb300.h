@@ -59,6 +59,10 @@ typedef struct {
     uint32_t max_batch_reads;    /* capacity hints; 0 = defaults. Larger batches return FP_BAD_INPUT */
     uint64_t max_batch_bases;
     uint64_t max_batch_cigar_ops;
+    uint32_t replay_reads_per_warp;  /* FP32 mode: reads per warp of the FP64 replay kernels, 1..32
+                                        (0 = default). Fewer reads per warp spread a small replay set over
+                                        more of the GPU's FP64 units */
+    uint32_t reserved;
 } fp_options;
 
 /* One alignment batch, mirroring alignment_batch_storage<host> (alignment_data.h:125-173). The engine
