@@ -77,7 +77,8 @@ double gaussian(double value) {  // device/empirical_quality.cu:43-53
 struct fp_engine {
     int device = 0;
     int baq_mode = FP_BAQ_FP32;
-    u32 replay_rpw = 32;  // reads per warp of the FP64 replay kernels
+    u32 replay_rpw = 0;  // FP64 replay: 0 = warp-cooperative kernel, 1..32 = thread-per-read, reads per warp
+    u32 flags = 0;       // FP_FLAG_*
     uint32_t n_rg = 1;
     cudaStream_t st = nullptr;
     std::string err;
@@ -182,6 +183,7 @@ fp_status fp_engine_create(const fp_options *o, fp_engine **out) {
     eng->device = o->device;
     eng->baq_mode = o->baq_mode;
     if (o->replay_reads_per_warp) eng->replay_rpw = o->replay_reads_per_warp;
+    eng->flags = o->flags;
     eng->n_rg = o->num_read_groups;
     cudaError_t e = cudaSetDevice(eng->device);
     if (e != cudaSuccess) {
@@ -202,6 +204,7 @@ fp_status fp_engine_create(const fp_options *o, fp_engine **out) {
     eng->hmm.gap_open = pow(10.0, (-40.0) / 10.);
     baq64_set_constants(eng->hmm);
     baq_tpr_set_constants(eng->hmm);
+    baq_exact_set_constants(eng->hmm);
     EmpConst ec;
     for (int d = 0; d <= 40; d++) ec.prior[d] = log10(gaussian(double(d)));
     for (int bin = 0; bin <= 60; bin++) {
@@ -477,12 +480,17 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
             if (c == 0) { cudaEventRecord(eng->ev[11], st); timed_main = true; }
             launch_cap(b, w, w.baq_list + size_t(c) * R, w.counters + c, 0, st, n_cls[c]);
         }
+        const bool replay_all = (eng->flags & FP_FLAG_REPLAY_ALL) != 0;
         for (int c = 0; c < 2; c++) {
             if (!n_cls[c]) continue;
-            const u32 *esc = w.esc_list + size_t(c) * R;
-            u32 *esc_count = w.counters + (c ? 10 : 4);
-            launch_baq_tpr(b, eng->ref, w, esc, esc_count, n_cls[c], c, true, w.counters + 11, eng->s32.p, budget,
-                           max_q, eng->replay_rpw, st);
+            const u32 *esc = replay_all ? w.baq_list + size_t(c) * R : w.esc_list + size_t(c) * R;
+            u32 *esc_count = replay_all ? w.counters + c : w.counters + (c ? 10 : 4);
+            if (eng->replay_rpw)
+                launch_baq_tpr(b, eng->ref, w, esc, esc_count, n_cls[c], c, true, w.counters + 11, eng->s32.p,
+                               budget, max_q, eng->replay_rpw, st);
+            else
+                launch_baq_exact(b, eng->ref, w, esc, esc_count, n_cls[c], c, w.counters + 11, eng->s32.p, budget,
+                                 max_q, st);
             launch_cap(b, w, esc, esc_count, 1, st, n_cls[c]);
         }
         if ((s = run_fp64(w.baq_list + 2ull * R, w.counters + 2, n_cls[2], bw_max[2])) != FP_OK) return s;

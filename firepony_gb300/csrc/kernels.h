@@ -76,6 +76,11 @@ u32 baq64_threads();
 
 // k_baq_tpr.cu (thread per read, band in registers; FP32 certified or exact FP64)
 void baq_tpr_set_constants(const HmmConst &c);
+// k_baq_exact.cu (exact FP64 replay, a group of lanes per read)
+void baq_exact_set_constants(const HmmConst &c);
+void launch_baq_exact(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
+                      u32 max_reads, int band_class, u32 *ctr, void *scratch, u64 scratch_bytes, u32 max_q,
+                      cudaStream_t s);
 void launch_baq_tpr(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
                     u32 max_reads, int band_class, bool exact, u32 *ctr, void *scratch, u64 scratch_bytes, u32 max_q,
                     u32 reads_per_warp, cudaStream_t s);

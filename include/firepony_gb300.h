@@ -62,8 +62,12 @@ typedef struct {
     uint32_t replay_reads_per_warp;  /* FP32 mode: reads per warp of the FP64 replay kernels, 1..32
                                         (0 = default). Fewer reads per warp spread a small replay set over
                                         more of the GPU's FP64 units */
-    uint32_t reserved;
+    uint32_t flags;              /* FP_FLAG_* bits (0 for normal operation) */
 } fp_options;
+
+/* Test hook: in FP32 mode, run every BAQ read of band width <= 15 through the exact FP64 replay as well
+ * (the replay's results replace the FP32 ones), so the replay kernels see the whole workload. */
+#define FP_FLAG_REPLAY_ALL 1u
 
 /* One alignment batch, mirroring alignment_batch_storage<host> (alignment_data.h:125-173). The engine
  * borrows these host buffers only for the duration of fp_engine_submit_batch. */

@@ -14,9 +14,9 @@ pytestmark = pytest.mark.gpu
 REL_TOL = 1e-9
 
 
-def run_engine(ref_or_contigs, batches, n_rg, mode, sites=None, replay_reads_per_warp=0):
+def run_engine(ref_or_contigs, batches, n_rg, mode, sites=None, replay_reads_per_warp=0, flags=0):
     from firepony_gb300.engine import Engine
-    e = Engine(num_read_groups=n_rg, baq_mode=mode, replay_reads_per_warp=replay_reads_per_warp)
+    e = Engine(num_read_groups=n_rg, baq_mode=mode, replay_reads_per_warp=replay_reads_per_warp, flags=flags)
     if sites is None:
         e.load_reference(ref_or_contigs)
     else:
@@ -206,3 +206,25 @@ def test_large_batch_properties(native):
     for k in range(4):
         assert np.all(np.diff(t[k]["keys"].astype(np.int64)) > 0)
     assert s["total_reads"] == 1_000_000
+
+
+@pytest.mark.parametrize("rpw", [0, 32])
+def test_replay_all_reads_exact(native, rpw):
+    """Every BAQ read through the exact FP64 replay (warp-cooperative kernel, or thread-per-read with rpw)."""
+    from firepony_gb300.abi import FP_FLAG_REPLAY_ALL
+    p, ref, batches = make_dataset("precision_20M_151bp_pe", 6000, 3000, 400_000)
+    te, se, ge = run_engine(ref, batches, p.num_read_groups, "fp32", replay_reads_per_warp=rpw,
+                            flags=FP_FLAG_REPLAY_ALL)
+    to, so, go = run_oracle(ref, batches, p.num_read_groups)
+    assert_stages_equal(batches[-1], ge, go)
+    assert_tables_equal(te, to)
+
+
+def test_replay_all_edge_cases(native):
+    from firepony_gb300.abi import FP_FLAG_REPLAY_ALL
+    from tests.edge_cases import edge_case_dataset
+    contigs, sites, batch, n_rg = edge_case_dataset()
+    te, se, ge = run_engine(contigs, [batch], n_rg, "fp32", sites, flags=FP_FLAG_REPLAY_ALL)
+    to, so, go = run_oracle(contigs, [batch], n_rg, sites)
+    assert_stages_equal(batch, ge, go)
+    assert_tables_equal(te, to)
