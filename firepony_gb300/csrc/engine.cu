@@ -81,6 +81,8 @@ struct fp_engine {
     u32 flags = 0;       // FP_FLAG_*
     uint32_t n_rg = 1;
     cudaStream_t st = nullptr;
+    cudaStream_t st2 = nullptr;          // band-class-1 BAQ, concurrent with class 0
+    cudaEvent_t fork = nullptr, join = nullptr;
     std::string err;
     bool finalized = false;
 
@@ -102,7 +104,7 @@ struct fp_engine {
     DevBuf in_buf;
     DevBatch batch{};
     DevBuf oplen, cigoff, ev_rc, ev_type, per_read, per_base, lists, counters, entry_cnt, entry_off;
-    DevBuf entries, entries_alt, sort_tmp, scan_tmp, s32, s64;
+    DevBuf entries, entries_alt, sort_tmp, scan_tmp, s32, s32b, s64;
     u64 s64_doubles = 0;
     BatchWork work{};
     uint32_t last_R = 0;
@@ -191,8 +193,11 @@ fp_status fp_engine_create(const fp_options *o, fp_engine **out) {
         return FP_DEVICE_ERROR;
     }
     e = cudaStreamCreateWithFlags(&eng->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&eng->st2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&eng->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&eng->join, cudaEventDisableTiming);
     if (e != cudaSuccess) {
-        delete eng;
+        fp_engine_destroy(eng);
         return FP_DEVICE_ERROR;
     }
     for (auto &x : eng->ev) cudaEventCreate(&x);
@@ -232,15 +237,19 @@ void fp_engine_destroy(fp_engine *eng) {
     if (!eng) return;
     cudaSetDevice(eng->device);
     if (eng->st) cudaStreamSynchronize(eng->st);
+    if (eng->st2) cudaStreamSynchronize(eng->st2);
     for (auto &b : eng->contig_bufs) b.release();
     for (auto &b : eng->site_bufs) b.release();
     DevBuf *bufs[] = {&eng->d_contigs, &eng->d_sites, &eng->tab_obs, &eng->tab_mism, &eng->tab_stage, &eng->in_buf, &eng->oplen,
                       &eng->cigoff, &eng->ev_rc, &eng->ev_type, &eng->per_read, &eng->per_base, &eng->lists,
                       &eng->counters, &eng->entry_cnt, &eng->entry_off, &eng->entries, &eng->entries_alt,
-                      &eng->sort_tmp, &eng->scan_tmp, &eng->s32, &eng->s64};
+                      &eng->sort_tmp, &eng->scan_tmp, &eng->s32, &eng->s32b, &eng->s64};
     for (DevBuf *b : bufs) b->release();
     for (auto &x : eng->ev)
         if (x) cudaEventDestroy(x);
+    if (eng->fork) cudaEventDestroy(eng->fork);
+    if (eng->join) cudaEventDestroy(eng->join);
+    if (eng->st2) cudaStreamDestroy(eng->st2);
     if (eng->st) cudaStreamDestroy(eng->st);
     delete eng;
 }
@@ -469,30 +478,43 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
         }
     } else {
         // FP32 with certified bounds (band classes 0 and 1), exact FP64 replay of the undecided reads, and the
-        // thread-per-read FP64 kernel for bands wider than 15
-        const u64 budget = u64(3) << 30;
+        // thread-per-read FP64 kernel for bands wider than 15. Band class 1 (few reads, latency-bound kernels)
+        // runs on a second stream with its own scratch and work counters, alongside the class-0 kernels.
+        const u64 budget = u64(3) << 30, budget1 = u64(1) << 30;
         CK(eng->s32.ensure(budget), "BAQ scratch");
-        for (int c = 0; c < 2; c++) {
-            if (!n_cls[c]) continue;
-            if (c == 0) cudaEventRecord(eng->ev[10], st);
-            launch_baq_tpr(b, eng->ref, w, w.baq_list + size_t(c) * R, w.counters + c, n_cls[c], c, false,
-                           w.counters + 8 + c, eng->s32.p, budget, max_q, 32, st);
-            if (c == 0) { cudaEventRecord(eng->ev[11], st); timed_main = true; }
-            launch_cap(b, w, w.baq_list + size_t(c) * R, w.counters + c, 0, st, n_cls[c]);
-        }
         const bool replay_all = (eng->flags & FP_FLAG_REPLAY_ALL) != 0;
-        for (int c = 0; c < 2; c++) {
-            if (!n_cls[c]) continue;
-            const u32 *esc = replay_all ? w.baq_list + size_t(c) * R : w.esc_list + size_t(c) * R;
+        auto run_fp32 = [&](int c, cudaStream_t cs, void *scr, u64 scr_bytes, u32 *ctr) {
+            const u32 *list = w.baq_list + size_t(c) * R;
+            if (c == 0) cudaEventRecord(eng->ev[10], cs);
+            launch_baq_tpr(b, eng->ref, w, list, w.counters + c, n_cls[c], c, false, ctr, scr, scr_bytes, max_q, 32, cs);
+            if (c == 0) { cudaEventRecord(eng->ev[11], cs); timed_main = true; }
+            launch_cap(b, w, list, w.counters + c, 0, cs, n_cls[c]);
+        };
+        auto run_replay = [&](int c, cudaStream_t cs, void *scr, u64 scr_bytes, u32 *ctr) {
+            const u32 *list = w.baq_list + size_t(c) * R;
+            const u32 *esc = replay_all ? list : w.esc_list + size_t(c) * R;
             u32 *esc_count = replay_all ? w.counters + c : w.counters + (c ? 10 : 4);
             if (eng->replay_rpw)
-                launch_baq_tpr(b, eng->ref, w, esc, esc_count, n_cls[c], c, true, w.counters + 11, eng->s32.p,
-                               budget, max_q, eng->replay_rpw, st);
+                launch_baq_tpr(b, eng->ref, w, esc, esc_count, n_cls[c], c, true, ctr, scr, scr_bytes, max_q,
+                               eng->replay_rpw, cs);
             else
-                launch_baq_exact(b, eng->ref, w, esc, esc_count, n_cls[c], c, w.counters + 11, eng->s32.p, budget,
-                                 max_q, st);
-            launch_cap(b, w, esc, esc_count, 1, st, n_cls[c]);
+                launch_baq_exact(b, eng->ref, w, esc, esc_count, n_cls[c], c, ctr, scr, scr_bytes, max_q, cs);
+            launch_cap(b, w, esc, esc_count, 1, cs, n_cls[c]);
+        };
+        // the class-0 FP32 kernel fills the GPU; after it, the class-0 replay (latency-bound, few warps) and
+        // the whole class-1 path run side by side
+        if (n_cls[0]) run_fp32(0, st, eng->s32.p, budget, w.counters + 8);
+        const bool split = n_cls[1] > 0;
+        if (split) {
+            CK(eng->s32b.ensure(budget1), "BAQ scratch");
+            CK(cudaEventRecord(eng->fork, st), "fork");
+            CK(cudaStreamWaitEvent(eng->st2, eng->fork, 0), "fork");
+            run_fp32(1, eng->st2, eng->s32b.p, budget1, w.counters + 9);
+            run_replay(1, eng->st2, eng->s32b.p, budget1, w.counters + 24);
+            CK(cudaEventRecord(eng->join, eng->st2), "join");
         }
+        if (n_cls[0]) run_replay(0, st, eng->s32.p, budget, w.counters + 11);
+        if (split) CK(cudaStreamWaitEvent(st, eng->join, 0), "join");
         if ((s = run_fp64(w.baq_list + 2ull * R, w.counters + 2, n_cls[2], bw_max[2])) != FP_OK) return s;
     }
     CK(cudaGetLastError(), "BAQ launch");

@@ -1,6 +1,7 @@
 // K3: fractional errors (device/fractional_errors.cu:39-141), high-quality windows
 // (device/covariates.cu:215-246) and covariate keys (device/covariates.cu:50-103 with the bit packers of
-// device/covariates/bit_packers/*.h) — one thread per read, in two passes over the read's events:
+// device/covariates/bit_packers/*.h; the cycle key follows cycle_illumina.h:46-95 and the context key
+// context.h:106-174) — one warp per read, in two passes over the read's events:
 //   count: folds observation counts (order-free integers) into the dense tables with atomics and counts
 //          the read's entries with a nonzero mismatch value;
 //   emit:  writes those entries as packed 64-bit (dense key << 32 | float bits) in stream order
@@ -15,79 +16,6 @@ namespace {
 
 struct us2 { u16 x, y; };
 
-// calculateFractionalErrorArray for one error bit of the per-base flags
-__device__ void fractional_errors(const u8 *bf, const u8 *tag, int n, u8 bit, float *out, int stride) {
-    bool inBlock = false;
-    int bs = -1;
-    int iii;
-    auto block = [&](int last, int start) {
-        const int s0 = start - 1 > 0 ? start - 1 : 0;
-        int total = 0;
-        for (int j = s0; j <= last; j++) total += (bf[j] & bit) ? 1 : 0;
-        const double v = double(total) / double(last - s0 + 1);
-        for (int j = s0; j <= last; j++) out[j * stride] = float(v);
-    };
-    for (iii = 0; iii < n; iii++) {
-        if (tag[iii] == NO_BAQ_UNCERTAINTY) {
-            if (!inBlock) {
-                out[iii * stride] = (bf[iii] & bit) ? 1.0f : 0.0f;
-            } else {
-                block(iii, bs);
-                inBlock = false;
-                bs = -1;
-            }
-        } else {
-            inBlock = true;
-            if (bs == -1) bs = iii;
-        }
-    }
-    if (inBlock) block(iii - 1, bs);
-}
-
-struct ReadKeys {
-    u32 rg, qs, rs;
-    bool neg, paired_second;
-    us2 cw, hq;
-    const u32 *reads;
-};
-
-// covariate_Cycle_Illumina::encode (cycle_illumina.h:46-95)
-__device__ __forceinline__ void cycle_keys(const ReadKeys &k, int off, u32 &sub, u32 &ind) {
-    const int readLength = int(k.cw.y) - int(k.cw.x) + 1;
-    const int order = k.paired_second ? -1 : 1;
-    const int i = off - int(k.cw.x);
-    int cycle, inc;
-    if (k.neg) { cycle = readLength * order; inc = -order; }
-    else { cycle = order; inc = order; }
-    cycle += i * inc;
-    const int maxc = readLength - 4 - 1;
-    u32 res = u32(cycle < 0 ? -cycle : cycle) << 1;
-    if (cycle < 0) res++;
-    sub = res;
-    ind = (i < 4 || i > maxc) ? CYCLE_INVALID : res;
-}
-
-// covariate_Context::encode (context.h:106-174)
-__device__ __forceinline__ void context_keys(const ReadKeys &k, int off, u32 &cm, u32 &ci) {
-    cm = CONTEXT_INVALID;
-    ci = CONTEXT_INVALID;
-    const int dir = k.neg ? 1 : -1;
-    const int avail = k.neg ? int(k.hq.y) - off + 1 : off - int(k.hq.x) + 1;
-    const int nb = avail < 3 ? avail : 3;
-    if (nb < 2) return;
-    u32 ctx = 0;
-    int num = 0;
-    for (int j = 0, i = off; j < nb; j++, i += dir) {
-        const u8 bp = sym4(k.reads, u64(k.rs) + u32(i));
-        if (bp != IUPAC_A && bp != IUPAC_C && bp != IUPAC_T && bp != IUPAC_G) break;
-        ctx = (ctx << 2) | u32(31 - __clz(u32(bp)));
-        num++;
-    }
-    if (k.neg) ctx = ~ctx & ((1u << (num * 2)) - 1);
-    if (num >= 2) cm = ((ctx >> (num - 2) * 2) << 4) | 2;
-    if (num >= 3) ci = ((ctx >> (num - 3) * 2) << 4) | 3;
-}
-
 constexpr int COV_WARPS = 8;
 constexpr u32 FULL = 0xffffffffu;
 
@@ -97,6 +25,82 @@ struct CovSmem {
     u8 tag[512];
     u8 sym[512];
 };
+struct FracSmem {
+    u32 pre[512];   // window-relative prefix counts of the SNP / insertion / deletion bits (10 bits each)
+    i16 last[512];  // last base before j (window-relative) whose BQ tag is NO_BAQ_UNCERTAINTY, or -1
+};
+
+// calculateFractionalErrorArray (device/fractional_errors.cu:39-141) for the three error bits at once, in
+// parallel over the window. The reference walks the window once: a base whose BQ tag is
+// NO_BAQ_UNCERTAINTY outside a block takes its own error bit; a maximal run of other tags (a block) and
+// the bases on either side of it (the one before, and the closing one after if any) take the block's
+// average, a later block overwriting the shared base of an earlier one. For base j with last64 / next64
+// the nearest NO_BAQ_UNCERTAINTY bases before / after it (-1 / n when none):
+//   block member:                      range [max(last64, 0), min(next64, n - 1)]
+//   base before a block (j+1 member):  range [j, min(next64, n - 1)]
+//   closing base (j-1 member):         range [max(last64, 0), j]
+//   otherwise:                         its own bit
+// with the average double(bits in range) / double(range length) rounded to float, as in the reference.
+__device__ void fractional_errors_warp(const CovSmem &sm, FracSmem &fs, u32 wx, int n, float *frac, int lane) {
+    const u32 lt = (1u << lane) - 1;
+    u32 carry_pre = 0;
+    int carry_last = -1;
+    for (int c = 0; c < n; c += 32) {
+        const int j = c + lane;
+        const bool in = j < n;
+        const u8 bfv = in ? sm.bf[wx + j] : 0;
+        const bool m64 = in && sm.tag[wx + j] == NO_BAQ_UNCERTAINTY;
+        const u32 ms = __ballot_sync(FULL, bfv & BF_SNP), mi = __ballot_sync(FULL, bfv & BF_INS);
+        const u32 md = __ballot_sync(FULL, bfv & BF_DEL), m6 = __ballot_sync(FULL, m64);
+        const u32 pre = carry_pre + u32(__popc(ms & lt)) + (u32(__popc(mi & lt)) << 10) + (u32(__popc(md & lt)) << 20);
+        const u32 below = m6 & lt;
+        const int last = below ? c + 31 - __clz(below) : carry_last;
+        if (in) {
+            fs.pre[j] = pre;
+            fs.last[j] = i16(last);
+        }
+        carry_pre += u32(__popc(ms)) + (u32(__popc(mi)) << 10) + (u32(__popc(md)) << 20);
+        if (m6) carry_last = c + 31 - __clz(m6);
+    }
+    if (lane == 0) fs.pre[n] = carry_pre;
+    __syncwarp();
+    int carry_next = n;
+    for (int c = ((n - 1) / 32) * 32; c >= 0; c -= 32) {
+        const int j = c + lane;
+        const bool in = j < n;
+        const bool m64 = in && sm.tag[wx + j] == NO_BAQ_UNCERTAINTY;
+        const u32 m6 = __ballot_sync(FULL, m64);
+        const u32 above = m6 & ~((2u << lane) - 1u);
+        const int next = above ? c + __ffs(above) - 1 : carry_next;
+        if (in) {
+            int lo = -1, hi = -1;
+            if (!m64) {
+                lo = fs.last[j] > 0 ? fs.last[j] : 0;
+                hi = next < n - 1 ? next : n - 1;
+            } else if (j + 1 < n && sm.tag[wx + j + 1] != NO_BAQ_UNCERTAINTY) {
+                lo = j;
+                hi = next < n - 1 ? next : n - 1;
+            } else if (j >= 1 && sm.tag[wx + j - 1] != NO_BAQ_UNCERTAINTY) {
+                lo = fs.last[j] > 0 ? fs.last[j] : 0;
+                hi = j;
+            }
+            float *o = frac + size_t(j) * 3;
+            if (lo < 0) {
+                const u8 bfv = sm.bf[wx + j];
+                o[0] = (bfv & BF_SNP) ? 1.0f : 0.0f;
+                o[1] = (bfv & BF_INS) ? 1.0f : 0.0f;
+                o[2] = (bfv & BF_DEL) ? 1.0f : 0.0f;
+            } else {
+                const u32 d = fs.pre[hi + 1] - fs.pre[lo];
+                const double len = double(hi - lo + 1);
+                o[0] = float(double(d & 1023u) / len);
+                o[1] = float(double((d >> 10) & 1023u) / len);
+                o[2] = float(double(d >> 20) / len);
+            }
+        }
+        if (m6) carry_next = c + __ffs(m6) - 1;
+    }
+}
 
 __device__ __forceinline__ void context_keys_smem(const u8 *sym, bool neg, us2 hq, int off, u32 &cm, u32 &ci) {
     cm = CONTEXT_INVALID;
@@ -134,8 +138,10 @@ __device__ __forceinline__ void add_pair(u32 *cnt, u32 key, u32 n) {
 template <bool EMIT>
 __global__ void __launch_bounds__(COV_WARPS * 32) k_cov(DevBatch b, BatchWork w, Tables t) {
     __shared__ CovSmem smem[COV_WARPS];
+    __shared__ FracSmem fsmem[EMIT ? 1 : COV_WARPS];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     CovSmem &sm = smem[warp];
+    FracSmem &fs = fsmem[EMIT ? 0 : warp];
     const u32 lt = (1u << lane) - 1;
     const KeySpace ks = t.ks;
     for (u32 r = blockIdx.x * COV_WARPS + warp; r < b.R; r += gridDim.x * COV_WARPS) {
@@ -180,11 +186,7 @@ __global__ void __launch_bounds__(COV_WARPS * 32) k_cov(DevBatch b, BatchWork w,
                 w.win[size_t(r) * 8 + 6] = hq.x;
                 w.win[size_t(r) * 8 + 7] = hq.y;
             }
-            if (lane < 3) {
-                const u8 bit = lane == 0 ? BF_SNP : (lane == 1 ? BF_INS : BF_DEL);
-                fractional_errors(sm.bf + cw.x, sm.tag + cw.x, int(cw.y) - int(cw.x) + 1, bit,
-                                  frac + size_t(cw.x) * 3 + lane, 3);
-            }
+            fractional_errors_warp(sm, fs, cw.x, int(cw.y) - int(cw.x) + 1, frac + size_t(cw.x) * 3, lane);
             __syncwarp();
         } else {
             hq = us2{win[6], win[7]};

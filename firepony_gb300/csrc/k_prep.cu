@@ -13,6 +13,7 @@ namespace {
 struct us2 { u16 x, y; };
 struct ss2 { i16 x, y; };
 
+typedef long long i64;
 template <typename T> __device__ __forceinline__ T tmin(T a, T b) { return a < b ? a : b; }
 template <typename T> __device__ __forceinline__ T tmax(T a, T b) { return a > b ? a : b; }
 __device__ __forceinline__ u32 baq_abs(i32 v) { return v < 0 ? u32(-v) : u32(v); }  // device/baq.cu:84-87
@@ -573,12 +574,16 @@ __global__ void __launch_bounds__(128) k_prep(DevBatch b, DevRef ref, BatchWork 
             // the work unit of the BAQ kernels' throughput figures
             int refLen = int(hw.y) - int(hw.x) + 1;
             if (hw.x < 0 && rd.astart < baq_abs(hw.x)) refLen--;
-            const int qL = int(wcl.y) - int(wcl.x) + 1;
-            u64 cells = 0;
-            for (int i = 1; i <= qL; i++) {
-                const int lo = 1 > i - int(bw) ? 1 : i - int(bw), hi = refLen < i + int(bw) ? refLen : i + int(bw);
-                if (hi >= lo) cells += u64(hi - lo + 1);
-            }
+            // closed form of sum_i (min(refLen, i+bw) - max(1, i-bw) + 1); |refLen - qL| <= bw keeps every
+            // term non-negative
+            const i64 qL = int(wcl.y) - int(wcl.x) + 1, R = refLen, B = bw;
+            auto tri = [](i64 n) -> i64 { return n > 0 ? n * (n + 1) / 2 : 0; };
+            i64 sum_hi = tri(qL) + qL * B;
+            const i64 t0 = R - B + 1 > 1 ? R - B + 1 : 1;
+            if (t0 <= qL) sum_hi -= tri(qL + B - R) - tri(t0 - 1 + B - R);
+            const i64 m = qL < B ? qL : B;
+            const i64 sum_lo = tri(qL) - qL * B + (m * (B + 1) - tri(m));
+            const u64 cells = u64(sum_hi - sum_lo + qL);
             atomicAdd(reinterpret_cast<unsigned long long *>(w.counters + 16) + cls, (unsigned long long)cells);
             atomicAdd(&w.counters[6], 1u);
             atomicMax(&w.counters[7], u32(wcl.y - wcl.x + 1));

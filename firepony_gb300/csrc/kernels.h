@@ -32,7 +32,8 @@ struct BatchWork {
     u32 *counters;           // [0..2] list sizes per band class, [4]/[10] escalated reads of class 0/1,
                              // [5] filtered, [6] BAQ reads, [7] longest BAQ query, [8..9],[11] work counters,
                              // [12..14] widest band per class, [16..21] u64 band cells per class,
-                             // [22]/[23] escalations with an undecided MAP state / with undecided qualities only
+                             // [22]/[23] escalations with an undecided MAP state / with undecided qualities only,
+                             // [24] work counter of the class-1 replay
     u32 *esc_list;
     // covariate entries
     u32 *entry_count;        // per read + 1
