@@ -97,7 +97,7 @@ struct fp_engine {
 
     // tables
     Tables tables{};
-    DevBuf tab_obs, tab_mism, tab_stage;
+    DevBuf tab_obs, tab_mism, tab_stage, tab_cyc;
     u64 staged_bases = 0;  // bases counted into the u32 stage since the last merge
 
     // batch buffers
@@ -148,6 +148,10 @@ fp_status alloc_tables(fp_engine *eng) {
     CK(eng->tab_stage.ensure(n * sizeof(u32)), "table allocation");
     CK(cudaMemsetAsync(eng->tab_stage.p, 0, n * sizeof(u32), eng->st), "table clear");
     eng->tables.stage = eng->tab_stage.as<u32>();
+    const size_t nd = size_t(eng->n_rg) * 2 * CYC_DIFF_LEN;
+    CK(eng->tab_cyc.ensure(nd * sizeof(int)), "table allocation");
+    CK(cudaMemsetAsync(eng->tab_cyc.p, 0, nd * sizeof(int), eng->st), "table clear");
+    eng->tables.cyc_diff = eng->tab_cyc.as<int>();
     eng->staged_bases = 0;
     CK(cudaMemsetAsync(eng->tab_obs.p, 0, n * sizeof(unsigned long long), eng->st), "table clear");
     CK(cudaMemsetAsync(eng->tab_mism.p, 0, n * sizeof(float), eng->st), "table clear");
@@ -240,7 +244,7 @@ void fp_engine_destroy(fp_engine *eng) {
     if (eng->st2) cudaStreamSynchronize(eng->st2);
     for (auto &b : eng->contig_bufs) b.release();
     for (auto &b : eng->site_bufs) b.release();
-    DevBuf *bufs[] = {&eng->d_contigs, &eng->d_sites, &eng->tab_obs, &eng->tab_mism, &eng->tab_stage, &eng->in_buf, &eng->oplen,
+    DevBuf *bufs[] = {&eng->d_contigs, &eng->d_sites, &eng->tab_obs, &eng->tab_mism, &eng->tab_stage, &eng->tab_cyc, &eng->in_buf, &eng->oplen,
                       &eng->cigoff, &eng->ev_rc, &eng->ev_type, &eng->per_read, &eng->per_base, &eng->lists,
                       &eng->counters, &eng->entry_cnt, &eng->entry_off, &eng->entries, &eng->entries_alt,
                       &eng->sort_tmp, &eng->scan_tmp, &eng->s32, &eng->s32b, &eng->s64};
@@ -529,6 +533,7 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
     }
     eng->staged_bases += Q;
     launch_cov_count(b, w, eng->tables, st);
+    launch_cycle_pairs(eng->tables, st);
     launch_exclusive_scan(w.entry_count, w.entry_offset, R, eng->scan_tmp.p, st);
     u32 tail[2];
     CK(cudaMemcpyAsync(&tail[0], w.entry_offset + R, 4, cudaMemcpyDeviceToHost, st), "D2H");
@@ -769,6 +774,7 @@ fp_status fp_engine_reset(fp_engine *eng) {
     CK(cudaMemsetAsync(eng->tab_obs.p, 0, n * sizeof(unsigned long long), eng->st), "reset");
     CK(cudaMemsetAsync(eng->tab_mism.p, 0, n * sizeof(float), eng->st), "reset");
     CK(cudaMemsetAsync(eng->tab_stage.p, 0, n * sizeof(u32), eng->st), "reset");
+    CK(cudaMemsetAsync(eng->tab_cyc.p, 0, size_t(eng->n_rg) * 2 * CYC_DIFF_LEN * sizeof(int), eng->st), "reset");
     eng->staged_bases = 0;
     CK(cudaStreamSynchronize(eng->st), "reset");
     for (auto &t : eng->out) t = HostTable();

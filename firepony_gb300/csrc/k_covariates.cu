@@ -133,17 +133,30 @@ __device__ __forceinline__ void add_pair(u32 *cnt, u32 key, u32 n) {
     atomicAdd(reinterpret_cast<unsigned long long *>(cnt + key), (unsigned long long)n | ((unsigned long long)n << 32));
 }
 
+// Count-kernel counters privatised per block (when the read groups are few enough): the quality-table M
+// counters (n_rg x 256) and the context-table I/D pair counters (n_rg x 80, the I and D counts of a key are
+// equal), in dynamic shared memory, flushed with one global atomic per nonzero counter at the end.
+constexpr u32 HIST_MAX_RG = 8;
+__host__ __device__ constexpr u32 hist_words(u32 n_rg) { return n_rg <= HIST_MAX_RG ? n_rg * (256 + 80) : 0; }
+
 // One warp per read. Lanes stage the read's qualities, flags, BQ tags and bases in shared memory, then walk
 // the read's CIGAR events 32 at a time (lane = event).
 template <bool EMIT>
 __global__ void __launch_bounds__(COV_WARPS * 32) k_cov(DevBatch b, BatchWork w, Tables t) {
     __shared__ CovSmem smem[COV_WARPS];
     __shared__ FracSmem fsmem[EMIT ? 1 : COV_WARPS];
+    extern __shared__ u32 hist[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     CovSmem &sm = smem[warp];
     FracSmem &fs = fsmem[EMIT ? 0 : warp];
     const u32 lt = (1u << lane) - 1;
     const KeySpace ks = t.ks;
+    const u32 hw_n = EMIT ? 0 : hist_words(ks.n_rg);
+    u32 *hist_q = hist, *hist_x = hist + ks.n_rg * 256;
+    if (!EMIT) {
+        for (u32 i = threadIdx.x; i < hw_n; i += blockDim.x) hist[i] = 0;
+        __syncthreads();
+    }
     for (u32 r = blockIdx.x * COV_WARPS + warp; r < b.R; r += gridDim.x * COV_WARPS) {
         if (w.status[r] != RS_ACTIVE) {
             if (!EMIT && lane == 0) w.entry_count[r] = 0;
@@ -244,14 +257,36 @@ __global__ void __launch_bounds__(COV_WARPS * 32) k_cov(DevBatch b, BatchWork w,
             const u32 kx1 = vxi ? ks.context_base + ((rgq + 45) * CONTEXT_SPAN + context_rank(ci)) * EV_SLOTS + 2 : 0;
             const u32 kx2 = kx1 + 1;
             if (!EMIT) {
-                agg_add(t.stage, kq0, g, lane);
-                if (g) {
-                    atomicAdd(&t.stage[kc0], 1u);
-                    if (vci) add_pair(t.stage, kc1, 1u);
+                if (hw_n) {
+                    if (g) atomicAdd(&hist_q[rg * 256 + qm], 1u);
+                } else {
+                    agg_add(t.stage, kq0, g, lane);
+                }
+                if (g) atomicAdd(&t.stage[kc0], 1u);
+                // cycle I/D pairs: along a run of events on consecutive bases |cycle| moves by one, so a run
+                // is one range update of the (read group, cycle sign) difference array
+                {
+                    const bool gv = g && vci;
+                    const u32 gvm = __ballot_sync(FULL, gv);
+                    const u32 poff = __shfl_up_sync(FULL, u32(off), 1), noff = __shfl_down_sync(FULL, u32(off), 1);
+                    const bool pv = lane > 0 && ((gvm >> (lane - 1)) & 1u);
+                    const bool nv = lane < 31 && ((gvm >> (lane + 1)) & 1u);
+                    const bool run_start = gv && !(pv && poff + 1 == u32(off));
+                    const bool run_end = gv && !(nv && noff == u32(off) + 1);
+                    if (run_start || run_end) {
+                        const int i = int(off) - int(cw.x);
+                        const int a = neg ? readLength - i : 1 + i;  // |cycle|
+                        int *d = t.cyc_diff + (size_t(rg) * 2 + (second ? 1 : 0)) * CYC_DIFF_LEN;
+                        // forward strand: |cycle| rises along the run, reverse strand: it falls
+                        if (run_start) atomicAdd(d + (neg ? a + 1 : a), neg ? -1 : 1);
+                        if (run_end) atomicAdd(d + (neg ? a : a + 1), neg ? 1 : -1);
+                    }
                 }
                 agg_add(t.stage, kx0, g && vxm, lane);
-                // the I and D context keys of a base share the context value: aggregate once, add the pair
-                {
+                if (hw_n) {
+                    if (g && vxi) atomicAdd(&hist_x[rg * 80 + context_rank(ci)], 1u);
+                } else {
+                    // the I and D context keys of a base share the context value: aggregate once, add the pair
                     const u32 k = (g && vxi) ? kx1 : 0xFFFFFFFFu;
                     const u32 peers = __match_any_sync(FULL, k);
                     if (g && vxi && (__ffs(peers) - 1) == lane) add_pair(t.stage, kx1, u32(__popc(peers)));
@@ -304,6 +339,47 @@ __global__ void __launch_bounds__(COV_WARPS * 32) k_cov(DevBatch b, BatchWork w,
             }
         }
     }
+    if (!EMIT && hw_n) {
+        __syncthreads();
+        for (u32 i = threadIdx.x; i < ks.n_rg * 256; i += blockDim.x) {
+            const u32 v = hist_q[i];
+            if (v) atomicAdd(&t.stage[ks.qual_base + i * EV_SLOTS + 0], v);
+        }
+        for (u32 i = threadIdx.x; i < ks.n_rg * 80; i += blockDim.x) {
+            const u32 v = hist_x[i];
+            if (v) add_pair(t.stage, ks.context_base + (((i / 80) * Q_SPAN + 45) * CONTEXT_SPAN + i % 80) * EV_SLOTS + 2, v);
+        }
+    }
+}
+
+// folds the batch's cycle difference arrays into the cycle I/D counters and clears them: one warp per
+// (read group, cycle sign), a running sum over |cycle|
+__global__ void k_cycle_pairs(Tables t) {
+    const u32 wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (wid >= t.ks.n_rg * 2) return;
+    const u32 rg = wid >> 1, sign = wid & 1;
+    int *d = t.cyc_diff + size_t(wid) * CYC_DIFF_LEN;
+    int carry = 0;
+    for (u32 c = 0; c < CYC_DIFF_LEN; c += 32) {
+        const u32 a = c + lane;
+        int v = a < CYC_DIFF_LEN ? d[a] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(FULL, v, o);
+            if (int(lane) >= o) v += y;
+        }
+        const int n = carry + v;
+        carry += __shfl_sync(FULL, v, 31);
+        if (a < CYC_DIFF_LEN) {
+            d[a] = 0;
+            if (n > 0) {
+                const u32 res = (a << 1) | sign;
+                const u32 key = t.ks.cycle_base + ((rg * Q_SPAN + 45) * CYCLE_SPAN + res) * EV_SLOTS + 2;
+                t.stage[key] += u32(n);
+                t.stage[key + 1] += u32(n);
+            }
+        }
+    }
 }
 
 
@@ -330,7 +406,15 @@ void launch_cov_count(const DevBatch &b, const BatchWork &w, const Tables &t, cu
     if (!b.R) return;
     u32 blocks = (b.R + COV_WARPS - 1) / COV_WARPS;
     if (blocks > 152 * 16) blocks = 152 * 16;
-    k_cov<false><<<blocks, COV_WARPS * 32, 0, s>>>(b, w, t);
+    const size_t smem = size_t(hist_words(t.ks.n_rg)) * sizeof(u32);
+    if (smem) cudaFuncSetAttribute(k_cov<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    k_cov<false><<<blocks, COV_WARPS * 32, smem, s>>>(b, w, t);
+    g_kernel_launches++;
+}
+
+void launch_cycle_pairs(const Tables &t, cudaStream_t s) {
+    const u32 warps = t.ks.n_rg * 2;
+    k_cycle_pairs<<<(warps + 3) / 4, 128, 0, s>>>(t);
     g_kernel_launches++;
 }
 

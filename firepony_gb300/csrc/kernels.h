@@ -47,13 +47,20 @@ struct BatchWork {
     u32 *err;
 };
 
+// cycle-covariate I/D observation counts of a batch as range updates: per (read group, sign of the cycle)
+// a difference array over |cycle| (0..CYC_DIFF_LEN-1); a run of consecutive bases adds +1 at one end and -1
+// past the other
+constexpr u32 CYC_DIFF_LEN = 520;
+
 struct Tables {
     KeySpace ks;
     unsigned long long *obs;  // per dense key: observations (merged from stage)
     u32 *stage;               // per dense key: observations since the last merge
     float *mism;              // per dense key
+    int *cyc_diff;            // n_rg x 2 x CYC_DIFF_LEN, zero between batches
 };
 void launch_merge_stage(const Tables &t, cudaStream_t s);
+void launch_cycle_pairs(const Tables &t, cudaStream_t s);
 
 // HMM constants computed on the host with the platform libm (exactly the reference's host values)
 struct HmmConst {
