@@ -323,6 +323,7 @@ def main():
                 "baq_reads_by_band": res["stats"]["baq_reads_by_band"],
                 "baq_escalated_by_band": res["stats"]["baq_escalated_by_band"],
                 "baq_escalated_by_cause": res["stats"]["baq_escalated_by_cause"],
+                "baq_path_ms": [round(v, 3) for v in res["stats"]["baq_path_ms"]],
                 "e2e_tables_identical": bool(res["same"])}
         print(json.dumps(line))
     if world > 1:

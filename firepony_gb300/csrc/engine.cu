@@ -116,7 +116,7 @@ struct fp_engine {
     // statistics
     fp_stats stats{};
     unsigned long long launch_base = 0;
-    cudaEvent_t ev[12]{};  // [0..8] stage boundaries, [10..11] the band-class-0 BAQ launch
+    cudaEvent_t ev[16]{};  // [0..8] stage boundaries, [10..11] the band-class-0 BAQ launch, [12..15] BAQ paths
     HmmConst hmm{};
     double qual2err[256];
 
@@ -197,7 +197,13 @@ fp_status fp_engine_create(const fp_options *o, fp_engine **out) {
         return FP_DEVICE_ERROR;
     }
     e = cudaStreamCreateWithFlags(&eng->st, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&eng->st2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) {
+        // band class 1 runs beside class 0 on a higher-priority stream: its blocks are placed first as SM
+        // resources free up
+        int least = 0, greatest = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        e = cudaStreamCreateWithPriority(&eng->st2, cudaStreamNonBlocking, greatest);
+    }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&eng->fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&eng->join, cudaEventDisableTiming);
     if (e != cudaSuccess) {
@@ -473,7 +479,7 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
         return FP_OK;
     };
     fp_status s;
-    bool timed_main = false;
+    bool timed_main = false, timed_paths = false;
     if (eng->baq_mode == FP_BAQ_FP64) {
         for (int c = 0; c < 3; c++) {
             if (c == 0 && n_cls[0]) { cudaEventRecord(eng->ev[10], st); }
@@ -502,22 +508,37 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
                 launch_baq_tpr(b, eng->ref, w, esc, esc_count, n_cls[c], c, true, ctr, scr, scr_bytes, max_q,
                                eng->replay_rpw, cs);
             else
-                launch_baq_exact(b, eng->ref, w, esc, esc_count, n_cls[c], c, ctr, scr, scr_bytes, max_q, cs);
+                launch_baq_exact(b, eng->ref, w, esc, esc_count, n_cls[c], c, ctr, scr, scr_bytes, max_q, replay_all,
+                                 cs);
             launch_cap(b, w, esc, esc_count, 1, cs, n_cls[c]);
         };
-        // the class-0 FP32 kernel fills the GPU; after it, the class-0 replay (latency-bound, few warps) and
-        // the whole class-1 path run side by side
-        if (n_cls[0]) run_fp32(0, st, eng->s32.p, budget, w.counters + 8);
+        // the class-1 FP32 kernel (few reads, latency-bound) is queued first on the high-priority stream; the
+        // class-0 FP32 kernel then fills what is left of the GPU
         const bool split = n_cls[1] > 0;
         if (split) {
             CK(eng->s32b.ensure(budget1), "BAQ scratch");
             CK(cudaEventRecord(eng->fork, st), "fork");
             CK(cudaStreamWaitEvent(eng->st2, eng->fork, 0), "fork");
             run_fp32(1, eng->st2, eng->s32b.p, budget1, w.counters + 9);
+            cudaEventRecord(eng->ev[12], eng->st2);
+        }
+        if (n_cls[0]) {
+            run_fp32(0, st, eng->s32.p, budget, w.counters + 8);
+            cudaEventRecord(eng->ev[14], st);
+        }
+        if (split) {
+            // FP64 replays slow to a crawl beside the FP32 kernel (they share its pipes): the class-1 replay
+            // waits for it and then runs beside the class-0 replay
+            CK(cudaStreamWaitEvent(eng->st2, eng->ev[14], 0), "fork");
             run_replay(1, eng->st2, eng->s32b.p, budget1, w.counters + 24);
+            cudaEventRecord(eng->ev[13], eng->st2);
             CK(cudaEventRecord(eng->join, eng->st2), "join");
         }
-        if (n_cls[0]) run_replay(0, st, eng->s32.p, budget, w.counters + 11);
+        if (n_cls[0]) {
+            run_replay(0, st, eng->s32.p, budget, w.counters + 11);
+            cudaEventRecord(eng->ev[15], st);
+        }
+        timed_paths = split && n_cls[0];
         if (split) CK(cudaStreamWaitEvent(st, eng->join, 0), "join");
         if ((s = run_fp64(w.baq_list + 2ull * R, w.counters + 2, n_cls[2], bw_max[2])) != FP_OK) return s;
     }
@@ -588,6 +609,11 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
     eng->stats.baq_escalated_by_cause[1] += cause[1];
     eng->stats.baq_escalated_by_band[0] += tail[1];
     eng->stats.baq_escalated_by_band[1] += esc1;
+    if (timed_paths) {
+        const int ids[4] = {14, 15, 12, 13};
+        for (int k = 0; k < 4; k++)
+            if (cudaEventElapsedTime(&ms, eng->ev[3], eng->ev[ids[k]]) == cudaSuccess) eng->stats.baq_path_ms[k] += ms;
+    }
     if (timed_main && cudaEventElapsedTime(&ms, eng->ev[10], eng->ev[11]) == cudaSuccess) {
         eng->stats.baq_main_ms += ms;
         eng->stats.baq_main_launches++;

@@ -14,6 +14,11 @@
 // the reference's zero-initialised rows. All groups of a warp step through the same row loop (the longest
 // read of the warp); a group past its own read's rows computes zeros and writes nothing.
 //
+// A replayed read needs exact results only where the FP32 pass left a base undecided (baq_amb != 0): the
+// certified rows keep their FP32 MAP output, which agrees with the reference wherever the capping step
+// looks. The forward pass is complete; the backward pass runs from the last row down to the lowest
+// undecided row, and MAP runs on the undecided rows only (all rows with the test hook).
+//
 // Per group scratch (global): rows 0..max_q+1 of ROWD doubles: forward M (WC), forward I (WC), the forward
 // row sum (replaced by its reciprocal before the backward pass), and the row's MAP maximum and sum.
 #include "kernels.h"
@@ -26,7 +31,9 @@ __constant__ double cx_gap_open;
 namespace {
 
 constexpr u32 FULL = 0xffffffffu;
-constexpr int EX_THREADS = 128;
+// 64-thread blocks (80-96 registers a thread): a replay block fits in the registers an SM running three
+// blocks of the FP32 band-class-0 kernel leaves free, so a replay on another stream runs beside it
+constexpr int EX_THREADS = 64;
 
 __device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
@@ -34,7 +41,7 @@ __device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b
 template <int G, int NS>
 __global__ void __launch_bounds__(EX_THREADS) k_baq_exact(DevBatch b, DevRef dref, BatchWork w, const u32 *list,
                                                           const u32 *count, u32 *work_ctr, double *scratch,
-                                                          u32 max_q) {
+                                                          u32 max_q, int full) {
     constexpr int WC = G * NS;          // band slots per read
     constexpr int GPW = 32 / G;         // reads (groups) per warp
     constexpr int WPB = EX_THREADS / 32;
@@ -102,6 +109,23 @@ __global__ void __launch_bounds__(EX_THREADS) k_baq_exact(DevBatch b, DevRef dre
             return ref == rd ? s_em[q] : s_mis[q];
         };
         const int Qmax = int(__reduce_max_sync(FULL, u32(qL)));
+        // rows whose FP32 result was certified keep it (the capping step needs exactly the certified part):
+        // only undecided rows get an exact MAP, and the backward pass stops at the lowest of them (full: all)
+        int i_min = qL + 1;
+        if (has) {
+            if (full) {
+                i_min = 1;
+            } else {
+                for (int row = 1 + l; row <= qL; row += G)
+                    if (w.baq_amb[qual0 + u32(row - 1)]) { i_min = row; break; }
+            }
+        }
+#pragma unroll
+        for (int o = G / 2; o >= 1; o >>= 1) {
+            const int v = __shfl_xor_sync(FULL, i_min, o);
+            i_min = v < i_min ? v : i_min;
+        }
+        const int Tmax = int(__reduce_max_sync(FULL, u32(qL - i_min + 1 > 0 ? qL - i_min + 1 : 0)));
 
         const double dsM = 1.0 / (2 * (qL > 0 ? qL : 1) + 2);
         const double sM = dsM, sI = dsM;
@@ -259,14 +283,14 @@ __global__ void __launch_bounds__(EX_THREADS) k_baq_exact(DevBatch b, DevRef dre
                 QI[s + 1] = bIv[j];
             }
             // 1 / s[i] for the backward rows, in parallel over the rows
-            for (int row = 1 + l; row < qL; row += G) FROW(row)[2 * WC] = __ddiv_rn(1.0, FROW(row)[2 * WC]);
+            for (int row = i_min + l; row < qL; row += G) FROW(row)[2 * WC] = __ddiv_rn(1.0, FROW(row)[2 * WC]);
             __syncwarp();
         }
 
-        // ---- backward fused with MAP, rows qL..1 of every group (t steps back from its own last row) ----
-        for (int t = 0; t < Qmax; t++) {
+        // ---- backward fused with MAP, rows qL..i_min of every group (t steps back from its own last row) ----
+        for (int t = 0; t < Tmax; t++) {
             const int i = qL - t;
-            const bool act = i >= 1;
+            const bool act = i >= i_min;
             const int beg = 1 > i - bw ? 1 : i - bw;
             const int end = refLen < i + bw ? refLen : i + bw;
             const int x = i - bw > 0 ? i - bw : 0;
@@ -320,12 +344,14 @@ __global__ void __launch_bounds__(EX_THREADS) k_baq_exact(DevBatch b, DevRef dre
                 }
             }
             // ---- MAP for row i (device/baq.cu:619-681): first maximum in (k, M before I) order ----
+            const bool need = act && (full || w.baq_amb[qual0 + u32(i - 1)] != 0);
+            if (!__any_sync(FULL, need)) continue;
             unsigned long long best = 0;
             u32 best_k = 0xFFFFFFFFu;
 #pragma unroll
             for (int j = 0; j < NS; j++) {
                 const int s = l + j * G, k = s + x;
-                const bool inb = act && k >= beg && k <= end;
+                const bool inb = need && k >= beg && k <= end;
                 double zm = 0.0, zi = 0.0;
                 if (inb) {
                     zm = dm(FROW(i)[s], bMv[j]);
@@ -346,7 +372,7 @@ __global__ void __launch_bounds__(EX_THREADS) k_baq_exact(DevBatch b, DevRef dre
                 if (ob > best || (ob == best && ok < best_k)) { best = ob; best_k = ok; }
             }
             __syncwarp();
-            if (l == 0 && act) {
+            if (l == 0 && need) {
                 double sum = 0.0;
 #pragma unroll
                 for (int q = 0; q < 2 * WC; q++) sum = da(sum, X2[q]);
@@ -360,6 +386,7 @@ __global__ void __launch_bounds__(EX_THREADS) k_baq_exact(DevBatch b, DevRef dre
 
         // ---- MAP qualities, in parallel over the rows: (int)(-4.343 * log(1 - max/sum) + .499) ----
         for (int row = 1 + l; row <= qL; row += G) {
+            if (!full && !w.baq_amb[qual0 + u32(row - 1)]) continue;
             const double mx = FROW(row)[2 * WC + 1], sum = FROW(row)[2 * WC + 2];
             const double p = __ddiv_rn(mx, sum);
             const double tq = da(dm(-4.343, log(__dsub_rn(1.0, p))), 0.499);
@@ -374,7 +401,7 @@ __global__ void __launch_bounds__(EX_THREADS) k_baq_exact(DevBatch b, DevRef dre
 
 template <int G, int NS>
 void launch_g(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
-              u32 max_reads, u32 *ctr, double *scratch, u64 scratch_elems, u32 max_q, cudaStream_t s) {
+              u32 max_reads, u32 *ctr, double *scratch, u64 scratch_elems, u32 max_q, int full, cudaStream_t s) {
     constexpr int WC = G * NS, GPW = 32 / G;
     const u64 per_group = (u64(max_q) + 2) * (2 * WC + 3);
     const u64 groups = scratch_elems / per_group;
@@ -385,7 +412,7 @@ void launch_g(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u3
     if (blocks > 152 * 8) blocks = 152 * 8;
     if (blocks == 0) return;
     cudaMemsetAsync(ctr, 0, sizeof(u32), s);
-    k_baq_exact<G, NS><<<u32(blocks), EX_THREADS, 0, s>>>(b, ref, w, list, count, ctr, scratch, max_q);
+    k_baq_exact<G, NS><<<u32(blocks), EX_THREADS, 0, s>>>(b, ref, w, list, count, ctr, scratch, max_q, full);
     g_kernel_launches++;
 }
 
@@ -398,14 +425,16 @@ void baq_exact_set_constants(const HmmConst &c) {
 
 void launch_baq_exact(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
                       u32 max_reads, int band_class, u32 *ctr, void *scratch, u64 scratch_bytes, u32 max_q,
-                      cudaStream_t s) {
+                      bool all_rows, cudaStream_t s) {
     if (!max_reads) return;
     // band class 0 (bw <= 7, 15 slots): 8 lanes x 2 slots, 4 reads per warp; class 1 (bw <= 15, 31 slots):
     // 16 lanes x 2 slots, 2 reads per warp
     if (band_class == 0)
-        launch_g<8, 2>(b, ref, w, list, count, max_reads, ctr, (double *)scratch, scratch_bytes / 8, max_q, s);
+        launch_g<8, 2>(b, ref, w, list, count, max_reads, ctr, (double *)scratch, scratch_bytes / 8, max_q,
+                       all_rows ? 1 : 0, s);
     else
-        launch_g<16, 2>(b, ref, w, list, count, max_reads, ctr, (double *)scratch, scratch_bytes / 8, max_q, s);
+        launch_g<16, 2>(b, ref, w, list, count, max_reads, ctr, (double *)scratch, scratch_bytes / 8, max_q,
+                        all_rows ? 1 : 0, s);
 }
 
 }  // namespace fpg

@@ -605,7 +605,7 @@ __global__ void __launch_bounds__(128) k_prep(DevBatch b, DevRef ref, BatchWork 
 // capped value depends on one (an undecided quality of a base whose state is the match at its expected
 // position, or an undecided state whose candidates do not all give MIN_BASE_QUAL), the read goes to the
 // escalation list and nothing is written.
-__global__ void __launch_bounds__(256) k_cap(DevBatch b, BatchWork w, const u32 *list, const u32 *count, int exact) {
+__global__ void __launch_bounds__(64) k_cap(DevBatch b, BatchWork w, const u32 *list, const u32 *count, int exact) {
     constexpr u32 FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const u32 lt = (1u << lane) - 1;
@@ -767,9 +767,11 @@ void launch_prep(const DevBatch &b, const DevRef &ref, const BatchWork &w, cudaS
 void launch_cap(const DevBatch &b, const BatchWork &w, const u32 *list, const u32 *count, int exact, cudaStream_t s,
                 u32 max_reads) {
     if (!max_reads) return;
-    u32 blocks = (max_reads + 7) / 8;  // one warp per read, 8 warps per block
-    if (blocks > 152 * 16) blocks = 152 * 16;
-    k_cap<<<blocks, 256, 0, s>>>(b, w, list, count, exact);
+    // one warp per read, 2 warps per block: small blocks also fit beside the BAQ kernels of the other band
+    // class running on another stream
+    u32 blocks = (max_reads + 1) / 2;
+    if (blocks > 152 * 64) blocks = 152 * 64;
+    k_cap<<<blocks, 64, 0, s>>>(b, w, list, count, exact);
     g_kernel_launches++;
 }
 

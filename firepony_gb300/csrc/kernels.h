@@ -88,7 +88,7 @@ void baq_tpr_set_constants(const HmmConst &c);
 void baq_exact_set_constants(const HmmConst &c);
 void launch_baq_exact(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
                       u32 max_reads, int band_class, u32 *ctr, void *scratch, u64 scratch_bytes, u32 max_q,
-                      cudaStream_t s);
+                      bool all_rows, cudaStream_t s);
 void launch_baq_tpr(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
                     u32 max_reads, int band_class, bool exact, u32 *ctr, void *scratch, u64 scratch_bytes, u32 max_q,
                     u32 reads_per_warp, cudaStream_t s);

@@ -129,6 +129,9 @@ typedef struct {
     uint64_t baq_band_cells[3];          /* HMM band cells (row x in-band reference positions) per class */
     uint64_t baq_main_launches;          /* launches of the dominant BAQ kernel (band class 0, FP32 or FP64) */
     double   baq_main_ms;                /* their device time */
+    double   baq_path_ms[4];             /* FP32 mode, device time from the BAQ stage start to the end of: the
+                                            class-0 FP32 kernel + capping, the class-0 replay, the class-1
+                                            FP32 kernel + capping, the class-1 replay */
 } fp_stats;
 
 typedef enum {
