@@ -444,9 +444,11 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
         w.baq_alt = reinterpret_cast<u16 *>(p); p += al(Q * 2);
         w.frac = reinterpret_cast<float *>(p);
     }
-    CK(eng->lists.ensure(al(R * 4ull) * 5), "work lists");
+    CK(eng->lists.ensure(al(R * 4ull) * 7 + 4096), "work lists");
     w.baq_list = eng->lists.as<u32>();
     w.esc_list = w.baq_list + 3ull * R;
+    u32 *sorted_lists = w.baq_list + 5ull * R;  // classes 0 and 1 by query length
+    u32 *len_hist = w.baq_list + 7ull * R;
     CK(eng->entry_cnt.ensure(al((R + 1) * 4ull)), "entry counts");
     CK(eng->entry_off.ensure(al((R + 1) * 4ull)), "entry offsets");
     w.entry_count = eng->entry_cnt.as<u32>();
@@ -493,8 +495,9 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
         const u64 budget = u64(3) << 30, budget1 = u64(1) << 30;
         CK(eng->s32.ensure(budget), "BAQ scratch");
         const bool replay_all = (eng->flags & FP_FLAG_REPLAY_ALL) != 0;
+        launch_sort_baq_lists(w, R, std::max(n_cls[0], n_cls[1]), len_hist, sorted_lists, st);
         auto run_fp32 = [&](int c, cudaStream_t cs, void *scr, u64 scr_bytes, u32 *ctr) {
-            const u32 *list = w.baq_list + size_t(c) * R;
+            const u32 *list = sorted_lists + size_t(c) * R;
             if (c == 0) cudaEventRecord(eng->ev[10], cs);
             launch_baq_tpr(b, eng->ref, w, list, w.counters + c, n_cls[c], c, false, ctr, scr, scr_bytes, max_q, 32, cs);
             if (c == 0) { cudaEventRecord(eng->ev[11], cs); timed_main = true; }

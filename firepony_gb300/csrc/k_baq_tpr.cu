@@ -341,7 +341,17 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
             const int end = refLen < i + bw ? refLen : i + bw;
             const int x = i - bw > 0 ? i - bw : 0;
             // forward row i (for MAP) is loaded first: the backward arithmetic of the row runs while the loads
-            // are in flight
+            // are in flight. FP32: the warp's row i - 3 (contiguous, all lanes) is pulled into L2 ahead of use
+            // by one bulk prefetch (the lists are ordered by query length, so a warp's lanes share rows)
+            if constexpr (!EXACT) {
+                const u32 am = __activemask();
+                if (i > 3 && lane == __ffs(am) - 1) {
+                    const T *wrow = scratch + (u64(gwarp) * (u64(max_q) + 2) + u64(i - 3)) * row_words * 32;
+                    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(wrow),
+                                 "r"(u32(row_words * 32 * sizeof(T)))
+                                 : "memory");
+                }
+            }
             T fM[W], fI[W];
 #pragma unroll
             for (int s = 0; s < W; s++) {

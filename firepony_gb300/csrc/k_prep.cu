@@ -764,6 +764,84 @@ void launch_prep(const DevBatch &b, const DevRef &ref, const BatchWork &w, cudaS
     g_kernel_launches++;
 }
 
+// ---------------------------------------------------------------------------------------------------
+// BAQ work lists ordered by HMM query length (longest first), a counting sort over the two FP32 band
+// classes: the 32 reads a warp of the thread-per-read kernels takes then walk the same rows, so their
+// scratch rows coalesce and their loops stay converged. Bins: class * 512 + (511 - query length).
+namespace {
+
+__device__ __forceinline__ u32 qlen_bin(const BatchWork &w, u32 r, u32 cls) {
+    const u16 *win = w.win + size_t(r) * 8;
+    return cls * 512u + (511u - u32(win[1] - win[0] + 1));
+}
+
+__global__ void k_len_hist(BatchWork w, u32 R, u32 *hist) {
+    __shared__ u32 h[1024];
+    for (u32 i = threadIdx.x; i < 1024; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    for (u32 cls = 0; cls < 2; cls++) {
+        const u32 n = w.counters[cls];
+        const u32 *list = w.baq_list + size_t(cls) * R;
+        for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+            atomicAdd(&h[qlen_bin(w, list[i], cls)], 1u);
+    }
+    __syncthreads();
+    for (u32 i = threadIdx.x; i < 1024; i += blockDim.x)
+        if (h[i]) atomicAdd(&hist[i], h[i]);
+}
+
+// exclusive scan of the 1024 bins in place, restarting at each class (one block of 1024 threads)
+__global__ void k_len_scan(u32 *hist) {
+    __shared__ u32 v[1024];
+    const u32 t = threadIdx.x;
+    v[t] = hist[t];
+    __syncthreads();
+    for (u32 o = 1; o < 512; o <<= 1) {
+        const u32 add = (t % 512) >= o ? v[t - o] : 0u;
+        __syncthreads();
+        v[t] += add;
+        __syncthreads();
+    }
+    hist[t] = v[t] - hist[t];
+}
+
+__global__ void k_len_scatter(BatchWork w, u32 R, u32 *offs, u32 *sorted) {
+    constexpr u32 FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    for (u32 cls = 0; cls < 2; cls++) {
+        const u32 n = w.counters[cls];
+        const u32 *list = w.baq_list + size_t(cls) * R;
+        u32 *out = sorted + size_t(cls) * R;
+        // the grid-stride loop runs the same trip count on every lane of a warp (lanes past n idle)
+        const u32 stride = gridDim.x * blockDim.x;
+        for (u32 base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
+            const u32 i = base + lane;
+            const bool in = i < n;
+            const u32 r = in ? list[i] : 0;
+            const u32 bin = in ? qlen_bin(w, r, cls) : 0xFFFFFFFFu;
+            const u32 peers = __match_any_sync(FULL, bin);
+            const int leader = __ffs(peers) - 1;
+            u32 pos = 0;
+            if (in && lane == leader) pos = atomicAdd(&offs[bin], u32(__popc(peers)));
+            pos = __shfl_sync(FULL, pos, leader);
+            if (in) out[pos + u32(__popc(peers & ((1u << lane) - 1)))] = r;
+        }
+    }
+}
+
+}  // namespace
+
+void launch_sort_baq_lists(const BatchWork &w, u32 R, u32 max_class_reads, u32 *hist, u32 *sorted, cudaStream_t s) {
+    if (!max_class_reads) return;
+    cudaMemsetAsync(hist, 0, 1024 * sizeof(u32), s);
+    u32 blocks = (max_class_reads + 255) / 256;
+    if (blocks > 152 * 4) blocks = 152 * 4;
+    k_len_hist<<<blocks, 256, 0, s>>>(w, R, hist);
+    k_len_scan<<<1, 1024, 0, s>>>(hist);
+    k_len_scatter<<<blocks, 256, 0, s>>>(w, R, hist, sorted);
+    g_kernel_launches += 3;
+}
+
 void launch_cap(const DevBatch &b, const BatchWork &w, const u32 *list, const u32 *count, int exact, cudaStream_t s,
                 u32 max_reads) {
     if (!max_reads) return;

@@ -72,6 +72,8 @@ struct HmmConst {
 void launch_validate(const DevBatch &b, u32 n_rg, u32 *err, cudaStream_t s);
 void launch_op_lengths(const DevBatch &b, u32 *out, cudaStream_t s);
 void launch_prep(const DevBatch &b, const DevRef &ref, const BatchWork &w, cudaStream_t s);
+// BAQ lists of band classes 0 and 1 ordered by query length into sorted (2 x R entries); hist: 1024 words
+void launch_sort_baq_lists(const BatchWork &w, u32 R, u32 max_class_reads, u32 *hist, u32 *sorted, cudaStream_t s);
 void launch_cap(const DevBatch &b, const BatchWork &w, const u32 *list, const u32 *count, int exact,
                 cudaStream_t s, u32 max_reads);
 
