@@ -48,6 +48,11 @@ def parse():
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--replay-rpw", type=int, default=0, help="reads per warp of the FP64 replay kernels (0: default)")
+    ap.add_argument("--plain-steps", type=int, default=2, help="batches through the plain FP64 path (0: skip)")
+    ap.add_argument("--serve-jobs", type=int, default=128, help="jobs of the serving measurement (0: skip)")
+    ap.add_argument("--serve-rate", type=float, default=20.0, help="job arrivals per second (Poisson)")
+    ap.add_argument("--serve-slots", type=int, default=2, help="engines of the job server")
+    ap.add_argument("--serve-max-reads", type=int, default=5_000_000, help="largest job (log-uniform from 1000)")
     return ap.parse_args()
 
 
@@ -100,6 +105,72 @@ def make_workload(num_batches, batch_reads):
     with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
         batches = list(ex.map(lambda i: ref.batch(i, batch_reads), range(num_batches)))
     return p, ref, batches
+
+
+def run_plain(args, res):
+    """The plain path (every BAQ read in exact FP64, FP_BAQ_FP64) on the first batches of the same workload,
+    inputs resident in HBM, CUDA events on the engine's stream."""
+    import torch
+    from firepony_gb300.engine import Engine
+    n = min(args.plain_steps, len(res["batches"]))
+    p = res["ref"].preset
+    eng = Engine(num_read_groups=p.num_read_groups, baq_mode="fp64")
+    eng.load_reference(res["ref"])
+    stream = torch.cuda.ExternalStream(eng.stream)
+    dev = [to_device(b) for b in res["batches"][:n]]
+    eng.submit_device_view(dev[0][1])  # warm-up
+    eng.finalize()
+    eng.reset()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _, v in dev:
+        eng.submit_device_view(v)
+    eng.finalize()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    eng.close()
+    reads = n * args.batch_reads
+    return {"value": reads / (ms / 1e3), "unit": "reads/s", "baq": "fp64 (every BAQ read exact FP64)",
+            "steps": n, "ms_per_step": ms / n}
+
+
+def run_serving(args):
+    """Recalibration jobs arriving as a Poisson process (the serving configuration: 3 contigs / 250 Mbp,
+    500k known sites, reads of 101 or 151 bp, 8 read groups) on the job server; each job is the first `size`
+    reads of a pinned pool, submitted through the C ABI from host memory. Latency = arrival to finished
+    tables."""
+    import numpy as np
+    from firepony_gb300 import synth
+    from firepony_gb300.engine import PinnedBatch
+    from firepony_gb300.serve import JobServer, jobs_from_pool, poisson_schedule, run_schedule
+    p = synth.PRESETS["serving_mixed"]
+    ref = synth.Reference(p)
+    per = 1_000_000
+    nb = (args.serve_max_reads + per - 1) // per
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+        host = list(ex.map(lambda i: ref.batch(i, per), range(nb)))
+    pinned = [PinnedBatch(b) for b in host]
+    del host
+    pool = [pb.batch for pb in pinned]
+    arrivals, sizes = poisson_schedule(args.serve_jobs, args.serve_rate, 1000, args.serve_max_reads, seed=3)
+    server = JobServer(ref, p.num_read_groups, slots=args.serve_slots)
+    try:
+        run_schedule(server, jobs_from_pool(pool, [20_000] * (2 * args.serve_slots), per), [0.0] * (2 * args.serve_slots))
+        res = run_schedule(server, jobs_from_pool(pool, sizes, per), arrivals)
+    finally:
+        server.close()
+        for pb in pinned:
+            pb.close()
+    lat = np.array([r.latency for r in res]) * 1e3
+    span = max(r.done for r in res) - min(r.arrival for r in res)
+    reads = int(sum(r.num_reads for r in res))
+    return {"workload": "serving_mixed: 3 contigs / 250 Mbp, 450k SNP + 50k indel sites, 101/151 bp reads, 8 read groups",
+            "jobs": len(res), "arrivals": f"Poisson {args.serve_rate:g}/s", "sizes": f"log-uniform 1000-{args.serve_max_reads} reads",
+            "slots": args.serve_slots, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(lat.mean()), "max_ms": float(lat.max()), "reads": reads, "reads_per_s": reads / span,
+            "errors": sum(1 for r in res if r.error)}
 
 
 def cpu_baseline(ref, batches, seconds):
@@ -305,6 +376,8 @@ def main():
         cpu = None
         if not args.no_cpu_baseline and world == 1:
             cpu = cpu_baseline(res["ref"], res["batches"], args.cpu_sample_seconds)
+        plain = run_plain(args, res) if args.plain_steps > 0 and world == 1 and args.baq == "fp32" else None
+        serving = run_serving(args) if args.serve_jobs > 0 and world == 1 else None
         line = {"metric": METRIC, "value": value, "unit": "reads/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
@@ -316,6 +389,8 @@ def main():
                 "gpu_launches": res["launches"],
                 "roofline": roofline(res, args),
                 "cpu_baseline": cpu,
+                "plain": plain,
+                "serving": serving,
                 "clocks": res["clocks"],
                 "stage_ms": [round(x, 3) for x in res["stage_ms"]],
                 "baq_reads": res["stats"]["baq_reads"],

@@ -1,0 +1,155 @@
+"""Job server over the C ABI: recalibration jobs arriving over time, each turned into its own tables.
+
+The reference runs one job per process (firepony.cu:300-420): it loads the reference and known sites,
+streams the job's batches through its pipelines and writes the report. A service answering many jobs
+keeps that state resident instead. `JobServer` holds `slots` engines (`fp_engine`), each with the
+reference contigs and known sites uploaded once, and a worker thread per engine that takes jobs from one
+FIFO queue: `fp_engine_reset` (tables to zero, residency kept), the job's batches through
+`fp_engine_submit_batch` (host buffers, copies included), `fp_engine_finalize`. Engines run on their own
+CUDA streams, so two jobs share the GPU when more than one is in flight. A job's latency is the time from
+its arrival (submission) to its finished tables.
+
+The ctypes calls release the GIL, so worker threads overlap host work (batch packing, result copies) with
+the device work of other jobs.
+"""
+from __future__ import annotations
+
+import queue
+import threading
+import time
+from dataclasses import dataclass, field
+from typing import Callable, Iterable
+
+import numpy as np
+
+from .engine import Engine
+
+
+@dataclass
+class Job:
+    """One recalibration job: its batches (host `synth.Batch`-like objects with `.view()`), produced lazily
+    by `batches()` so that packing happens on the worker thread, as an io thread would do it."""
+    job_id: int
+    num_reads: int
+    batches: Callable[[], Iterable]
+    arrival: float = 0.0
+
+
+@dataclass
+class JobResult:
+    job_id: int
+    num_reads: int
+    arrival: float
+    start: float
+    done: float
+    tables: dict | None = None
+    error: str | None = None
+
+    @property
+    def latency(self) -> float:
+        return self.done - self.arrival
+
+
+@dataclass
+class _Pending:
+    job: Job
+    event: threading.Event = field(default_factory=threading.Event)
+    result: JobResult | None = None
+
+
+class JobServer:
+    def __init__(self, reference, num_read_groups: int, slots: int = 2, baq_mode: str = "fp32", device: int = 0,
+                 keep_tables: bool = False):
+        self.keep_tables = keep_tables
+        self.engines = []
+        for _ in range(slots):
+            e = Engine(num_read_groups=num_read_groups, baq_mode=baq_mode, device=device)
+            e.load_reference(reference)
+            self.engines.append(e)
+        self._q: queue.Queue = queue.Queue()
+        self._threads = [threading.Thread(target=self._worker, args=(e,), daemon=True) for e in self.engines]
+        for t in self._threads:
+            t.start()
+
+    def submit(self, job: Job) -> _Pending:
+        job.arrival = time.perf_counter()
+        p = _Pending(job)
+        self._q.put(p)
+        return p
+
+    def _worker(self, eng: Engine):
+        while True:
+            p = self._q.get()
+            if p is None:
+                return
+            job = p.job
+            start = time.perf_counter()
+            try:
+                eng.reset()
+                for b in job.batches():
+                    eng.submit(b)
+                tables = eng.finalize()
+                p.result = JobResult(job.job_id, job.num_reads, job.arrival, start, time.perf_counter(),
+                                     tables if self.keep_tables else None)
+            except Exception as ex:  # the job fails, the server keeps running
+                p.result = JobResult(job.job_id, job.num_reads, job.arrival, start, time.perf_counter(),
+                                     error=str(ex))
+            p.event.set()
+
+    def close(self):
+        for _ in self._threads:
+            self._q.put(None)
+        for t in self._threads:
+            t.join()
+        for e in self.engines:
+            e.close()
+        self.engines = []
+
+
+def poisson_schedule(num_jobs: int, rate_per_s: float, min_reads: int, max_reads: int, seed: int):
+    """Arrival offsets (s) of a Poisson process and log-uniform job sizes (reads), seeded."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate_per_s, size=num_jobs)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    sizes = np.exp(rng.uniform(np.log(min_reads), np.log(max_reads), size=num_jobs)).astype(np.int64)
+    return arrivals, sizes
+
+
+def jobs_from_pool(pool: list, sizes, batch_reads: int) -> list[Job]:
+    """Jobs made of the first `size` reads of a pool of batches (read ranges of the pool's batches, at most
+    `batch_reads` reads per submitted batch)."""
+    cap = sum(b.num_reads for b in pool)
+    jobs = []
+    for j, size in enumerate(sizes):
+        size = int(min(size, cap))
+
+        def make(size=size):
+            left = size
+            for b in pool:
+                first = 0
+                while left > 0 and first < b.num_reads:
+                    n = min(left, batch_reads, b.num_reads - first)
+                    yield b.range(first, first + n)
+                    first += n
+                    left -= n
+                if left <= 0:
+                    return
+
+        jobs.append(Job(j, size, make))
+    return jobs
+
+
+def run_schedule(server: JobServer, jobs: list[Job], arrivals) -> list[JobResult]:
+    """Submits each job at its arrival offset (real time) and waits for all results."""
+    t0 = time.perf_counter()
+    pending = []
+    for job, at in zip(jobs, arrivals):
+        delay = t0 + float(at) - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        pending.append(server.submit(job))
+    out = []
+    for p in pending:
+        p.event.wait()
+        out.append(p.result)
+    return out

@@ -187,6 +187,40 @@ class Batch:
             setattr(v, name, a.ctypes.data_as(C.c_void_p))
         return v
 
+    def range(self, first: int, last: int) -> "Batch":
+        """Reads [first, last) as a batch that shares this batch's arrays (no copy of bases, qualities or
+        CIGARs): per-read arrays are views and the three start arrays are rebased. Reads of a generated batch
+        are stored in order, so their CIGARs, packed bases and qualities are contiguous ranges."""
+        a = self.arrays
+        if not 0 <= first <= last <= self.num_reads:
+            raise ValueError("read range outside the batch")
+        n = last - first
+        out = {}
+        for name in ("chromosome", "alignment_start", "alignment_stop", "mate_alignment_start",
+                     "inferred_insert_size", "flags", "mapq", "read_group", "read_len", "qual_len", "cigar_len"):
+            out[name] = a[name][first:last]
+        if n == 0:
+            for name, dt in (("cigars", np.uint32), ("reads", np.uint32), ("qualities", np.uint8)):
+                out[name] = np.zeros(0, dt)
+            for name in ("cigar_start", "read_start", "qual_start"):
+                out[name] = np.zeros(0, np.uint32)
+            return Batch(out, 0, 0, 0, 0)
+        c0 = int(a["cigar_start"][first])
+        c1 = int(a["cigar_start"][last - 1]) + int(a["cigar_len"][last - 1])
+        r0 = int(a["read_start"][first])
+        r1 = int(a["read_start"][last - 1]) + (int(a["read_len"][last - 1]) + 7) // 8 * 8
+        q0 = int(a["qual_start"][first])
+        q1 = int(a["qual_start"][last - 1]) + int(a["qual_len"][last - 1])
+        if r0 % 8:
+            raise ValueError("read start not on a packed-word boundary")
+        out["cigars"] = a["cigars"][c0:c1]
+        out["reads"] = a["reads"][r0 // 8:(r1 + 7) // 8]
+        out["qualities"] = a["qualities"][q0:q1]
+        out["cigar_start"] = (a["cigar_start"][first:last] - np.uint32(c0)).astype(np.uint32)
+        out["read_start"] = (a["read_start"][first:last] - np.uint32(r0)).astype(np.uint32)
+        out["qual_start"] = (a["qual_start"][first:last] - np.uint32(q0)).astype(np.uint32)
+        return Batch(out, n, c1 - c0, r1 - r0, q1 - q0)
+
     def subset(self, read_ids) -> "Batch":
         """A new self-contained batch holding the given reads (in the given order)."""
         read_ids = np.asarray(read_ids, dtype=np.int64)
