@@ -156,111 +156,6 @@ __device__ void alignment_window(const DevBatch &b, u32 r, u32 &wx, u32 &wy, u32
     }
 }
 
-// cigar_coordinates_expand (device/cigar.cu:536-614) + cigar_op_expand (:55-95)
-__device__ void expand_read(Read &rd) {
-    const DevBatch &b = rd.b;
-    u16 ro = 0, fo = 0;
-    u32 e = 0;
-    const u32 c0 = b.cigar_start[rd.r], c1 = c0 + b.cigar_len[rd.r];
-    for (u32 c = c0; c < c1; c++) {
-        const u32 v = b.cigars[c], op = op_code(v), len = op_len(v);
-        for (u32 i = 0; i < len; i++, e++) {
-            u32 rc;
-            u8 t;
-            switch (op) {
-            case OP_M: case OP_EQ: case OP_X: rc = u32(ro++) | (u32(fo++) << 16); t = EV_M; break;
-            case OP_S: rc = u32(ro++) | (u32(U16_NONE) << 16); t = EV_S; break;
-            case OP_N: case OP_I: rc = u32(ro++) | (u32(U16_NONE) << 16); t = EV_I; break;
-            default: rc = u32(U16_NONE) | (u32(fo++) << 16); t = EV_D; break;  // D, H, P
-            }
-            rd.rc[e] = rc;
-            rd.ty[e] = t;
-        }
-    }
-}
-
-// remove_adapters (device/cigar.cu:111-344). The backward walk for a left tail cannot leave the read: a
-// matched event without a read coordinate always follows the read's first read-coordinate event, because
-// the window check before it rejects boundaries left of the first aligned base.
-__device__ int read_coord_for_ref(const Read &rd, u32 ref_coord, bool right_tail) {
-    for (u32 ev = 0; ev < rd.n; ev++) {
-        if (rd.astart + u32(rd.refc(ev)) == ref_coord) {
-            u16 read_coord = rd.readc(ev);
-            if (read_coord == U16_NONE) {
-                if (right_tail) {
-                    while (ev < rd.n) {
-                        read_coord = rd.readc(ev);
-                        if (read_coord != U16_NONE) break;
-                        ev++;
-                    }
-                } else {
-                    while (ev > 0) {
-                        ev--;
-                        read_coord = rd.readc(ev);
-                        if (read_coord != U16_NONE) break;
-                    }
-                }
-                if (read_coord == U16_NONE) return -1;
-            }
-            return read_coord;
-        }
-    }
-    return -1;
-}
-
-__device__ us2 current_reference_window(const Read &rd, us2 w) {
-    us2 out = {0, 0};
-    for (u32 i = 0; i < rd.n; i++) {
-        if (rd.readc(i) == w.x) {
-            while (i < rd.n && rd.refc(i) == U16_NONE) i++;
-            if (i == rd.n) return us2{U16_NONE, U16_NONE};
-            out.x = rd.refc(i);
-            break;
-        }
-    }
-    for (int i = int(rd.n) - 1; i >= 0; i--) {
-        if (rd.readc(u32(i)) == w.y) {
-            while (rd.refc(u32(i)) == U16_NONE && i > 0) i--;
-            if (i == 0) return us2{U16_NONE, U16_NONE};
-            out.y = rd.refc(u32(i));
-            break;
-        }
-    }
-    return out;
-}
-
-__device__ void remove_adapters(const Read &rd, us2 &w) {
-    const DevBatch &b = rd.b;
-    const u32 r = rd.r;
-    const u32 flags = rd.flags;
-    const i32 isize = b.isize[r];
-    // hasWellDefinedFragmentSize (:117-146)
-    if (isize == 0) return;
-    if (!(flags & F_PAIRED)) return;
-    if ((flags & F_UNMAP) || (flags & F_MATE_UNMAP)) return;
-    const bool rev = flags & F_REVERSE, mate_rev = flags & F_MATE_REVERSE;
-    if (rev == mate_rev) return;
-    bool ok = rev ? (b.astop[r] > b.mstart[r]) : (rd.astart <= b.mstart[r] + u32(isize));
-    if (!ok) return;
-    // getAdaptorBoundary (:150-163)
-    u32 boundary;
-    if (rev) boundary = u32(b.mstart[r] - 1);
-    else boundary = u32(rd.astart + u32(isize < 0 ? -isize : isize) + 1u);
-    if (boundary == U32_NONE) return;
-    const us2 rw = current_reference_window(rd, w);
-    if (boundary < rd.astart + u32(rw.x) || boundary > rd.astart + u32(rw.y)) return;
-    if (rev) {
-        // hardClipByReferenceCoordinates with refStart = -1 (:251-266)
-        const int stop = read_coord_for_ref(rd, u32(int(boundary)), false);
-        w.x = tmax<u16>(w.x, u16(u16(stop) + 1));
-    } else {
-        int start;
-        if (int(boundary) < 0) start = 0;  // refStart < 0 branch
-        else start = read_coord_for_ref(rd, u32(int(boundary)), true);
-        w.y = tmin<u16>(w.y, u16(u16(start) - 1));
-    }
-}
-
 // remove_soft_clips (device/cigar.cu:346-408)
 __device__ void remove_soft_clips(const Read &rd, us2 &w) {
     const DevBatch &b = rd.b;
@@ -292,95 +187,6 @@ __device__ void remove_soft_clips(const Read &rd, us2 &w) {
     }
 }
 
-// compute_no_insertions_window (device/cigar.cu:410-471); (0xFFFF, 0xFFFF) when nothing qualifies
-__device__ us2 no_insertions_window(const Read &rd, us2 w) {
-    us2 out = {U16_NONE, U16_NONE};
-    for (u32 ev = 0; ev < rd.n; ev++) {
-        const u16 ro = rd.readc(ev);
-        if (ro == U16_NONE || ro < w.x) continue;
-        if (rd.ty[ev] == EV_I) continue;
-        out.x = ro;
-        break;
-    }
-    for (int ev = int(rd.n) - 1; ev >= 0; ev--) {
-        const u16 ro = rd.readc(u32(ev));
-        if (ro == U16_NONE || ro > w.y) continue;
-        if (rd.ty[ev] == EV_I) continue;
-        out.y = ro;
-        break;
-    }
-    return out;
-}
-
-// compute_reference_window (device/cigar.cu:473-534); same convention
-__device__ us2 reference_window(const Read &rd, us2 ni) {
-    us2 out = {U16_NONE, U16_NONE};
-    for (u32 i = 0; i < rd.n; i++) {
-        if (rd.readc(i) == ni.x) {
-            while (i < rd.n && rd.refc(i) == U16_NONE) i++;
-            if (i == rd.n) return us2{U16_NONE, U16_NONE};
-            out.x = rd.refc(i);
-            break;
-        }
-    }
-    for (int i = int(rd.n) - 1; i >= 0; i--) {
-        if (rd.readc(u32(i)) == ni.y) {
-            while (rd.refc(u32(i)) == U16_NONE && i > 0) i--;
-            if (i == 0) return us2{U16_NONE, U16_NONE};
-            out.y = rd.refc(u32(i));
-            break;
-        }
-    }
-    return out;
-}
-
-// compute_error_vectors (device/cigar.cu:616-737): only op codes M (0), I (1), D (2) count
-__device__ u16 error_vectors(const Read &rd, const DevContig *g, us2 w, us2 rw, u8 *bf) {
-    const DevBatch &b = rd.b;
-    const bool neg = rd.flags & F_REVERSE;
-    u16 cur = 0, nerr = 0;
-    const u32 c0 = b.cigar_start[rd.r], c1 = c0 + b.cigar_len[rd.r];
-    for (u32 c = c0; c < c1; c++) {
-        const u32 e0 = rd.w.cigar_offsets[c] - rd.cs, e1 = rd.w.cigar_offsets[c + 1] - rd.cs;
-        const u32 op = op_code(b.cigars[c]);
-        if (op == OP_M) {
-            for (u32 i = e0; i < e1; i++) {
-                cur = rd.readc(i);
-                const u8 rbp = rd.sym(cur);
-                const u8 fbp = contig_at(*g, u64(rd.astart) + rd.refc(i));
-                if (fbp != rbp) {
-                    bf[cur] |= BF_SNP;
-                    if (cur >= w.x && cur <= w.y) nerr++;
-                }
-            }
-        } else if (op == OP_I) {
-            cur = u16(rd.w.ev_rc[rd.cs + e0] & 0xFFFF);
-            if (cur >= w.x && cur <= w.y) {
-                const int off = neg ? int(cur) + int(op_len(b.cigars[c])) : int(cur) - 1;
-                if (off >= 0 && off <= int(w.y)) {
-                    bf[off] |= BF_INS;
-                    nerr++;
-                }
-            }
-        } else if (op == OP_D) {
-            const u16 cref = u16(rd.w.ev_rc[rd.cs + e0] >> 16);
-            if (cref >= rw.x && cref <= rw.y) {
-                if (!neg) {
-                    bf[cur] |= BF_DEL;
-                    nerr++;
-                } else {
-                    const u16 off = u16(cur + 1);
-                    if (off < rd.rlen) {
-                        bf[off] |= BF_DEL;
-                        nerr++;
-                    }
-                }
-            }
-        }
-    }
-    return nerr;
-}
-
 // lower_bound / upper_bound (device/primitives/algorithms.h:39-100)
 __device__ u32 ref_lower_bound(u32 x, const u32 *a, u32 n) {
     if (n == 0) return 0;
@@ -402,8 +208,209 @@ __device__ u32 ref_upper_bound(u32 x, const u32 *a, u32 n) {
     return base;
 }
 
-// compute_vcf_ranges + filter_bps (device/snp_filter.cu:162-395)
-__device__ void filter_known_sites(const Read &rd, us2 w, us2 rw, u8 *bf) {
+// ---------------------------------------------------------------------------------------------------
+// Warp-per-read forms of the event scans and per-base passes used by k_prep. Every lane of the warp holds
+// the same read-level scalars (computed redundantly, the loads are broadcasts); event searches are ballots
+// over 32 events at a time and per-event / per-base work is lane-strided.
+constexpr u32 WFULL = 0xffffffffu;
+
+// first event e in [lo, n) with pred(e), or n
+template <typename P> __device__ __forceinline__ u32 first_from(u32 lo, u32 n, int lane, P pred) {
+    for (u32 c = lo; c < n; c += 32) {
+        const u32 e = c + u32(lane);
+        const u32 m = __ballot_sync(WFULL, e < n && pred(e));
+        if (m) return c + __ffs(m) - 1;
+    }
+    return n;
+}
+// last event e in [0, hi) with pred(e), or -1
+template <typename P> __device__ __forceinline__ int last_below(int hi, int lane, P pred) {
+    for (int c = hi - 32; c > -32; c -= 32) {
+        const int e = c + lane;
+        const u32 m = __ballot_sync(WFULL, e >= 0 && e < hi && pred(u32(e)));
+        if (m) return c + 31 - __clz(m);
+    }
+    return -1;
+}
+
+// cigar_coordinates_expand (device/cigar.cu:536-614) + cigar_op_expand (:55-95): op by op, the op's events
+// lane-strided; read and reference offsets at the op start carried as scalars
+__device__ void expand_read_w(Read &rd, int lane) {
+    const DevBatch &b = rd.b;
+    u32 ro = 0, fo = 0, e = 0;
+    const u32 c0 = b.cigar_start[rd.r], c1 = c0 + b.cigar_len[rd.r];
+    for (u32 c = c0; c < c1; c++) {
+        const u32 v = b.cigars[c], op = op_code(v), len = op_len(v);
+        const bool reads_base = op == OP_M || op == OP_EQ || op == OP_X || op == OP_S || op == OP_N || op == OP_I;
+        const bool refs_base = op == OP_M || op == OP_EQ || op == OP_X || !reads_base;
+        for (u32 i = u32(lane); i < len; i += 32) {
+            u32 rcv;
+            u8 t;
+            if (op == OP_M || op == OP_EQ || op == OP_X) { rcv = u32(u16(ro + i)) | (u32(u16(fo + i)) << 16); t = EV_M; }
+            else if (op == OP_S) { rcv = u32(u16(ro + i)) | (u32(U16_NONE) << 16); t = EV_S; }
+            else if (op == OP_N || op == OP_I) { rcv = u32(u16(ro + i)) | (u32(U16_NONE) << 16); t = EV_I; }
+            else { rcv = u32(U16_NONE) | (u32(u16(fo + i)) << 16); t = EV_D; }  // D, H, P
+            rd.rc[e + i] = rcv;
+            rd.ty[e + i] = t;
+        }
+        if (reads_base) ro += len;
+        if (refs_base) fo += len;
+        e += len;
+    }
+    __syncwarp();
+}
+
+// remove_adapters' read coordinate search (device/cigar.cu:251-344); see read_coord_for_ref
+__device__ int read_coord_for_ref_w(const Read &rd, u32 ref_coord, bool right_tail, int lane) {
+    const u32 ev = first_from(0, rd.n, lane, [&](u32 e) { return rd.astart + u32(rd.refc(e)) == ref_coord; });
+    if (ev == rd.n) return -1;
+    u16 read_coord = rd.readc(ev);
+    if (read_coord == U16_NONE) {
+        if (right_tail) {
+            const u32 e2 = first_from(ev, rd.n, lane, [&](u32 e) { return rd.readc(e) != U16_NONE; });
+            if (e2 == rd.n) return -1;
+            read_coord = rd.readc(e2);
+        } else {
+            const int e2 = last_below(int(ev), lane, [&](u32 e) { return rd.readc(e) != U16_NONE; });
+            if (e2 < 0) return -1;
+            read_coord = rd.readc(u32(e2));
+        }
+    }
+    return read_coord;
+}
+
+// current_reference_window (device/cigar.cu:165-200, init (0, 0)) and compute_reference_window
+// (:473-534, init (0xFFFF, 0xFFFF)): the reference offsets of the first event at read offset a.x (or the
+// next event that has one) and of the last event at read offset a.y (or the previous one; reaching the first
+// event gives (0xFFFF, 0xFFFF))
+__device__ us2 ref_window_w(const Read &rd, us2 a, u16 init, int lane) {
+    us2 out = {init, init};
+    const u32 i = first_from(0, rd.n, lane, [&](u32 e) { return rd.readc(e) == a.x; });
+    if (i < rd.n) {
+        const u32 j = first_from(i, rd.n, lane, [&](u32 e) { return rd.refc(e) != U16_NONE; });
+        if (j == rd.n) return us2{U16_NONE, U16_NONE};
+        out.x = rd.refc(j);
+    }
+    const int k = last_below(int(rd.n), lane, [&](u32 e) { return rd.readc(e) == a.y; });
+    if (k >= 0) {
+        const int j = last_below(k + 1, lane, [&](u32 e) { return e >= 1 && rd.refc(e) != U16_NONE; });
+        if (j < 1) return us2{U16_NONE, U16_NONE};
+        out.y = rd.refc(u32(j));
+    }
+    return out;
+}
+
+// remove_adapters (device/cigar.cu:111-344). The backward walk for a left tail cannot leave the read: a
+// matched event without a read coordinate always follows the read's first read-coordinate event, because
+// the window check before it rejects boundaries left of the first aligned base.
+__device__ void remove_adapters_w(const Read &rd, us2 &w, int lane) {
+    const DevBatch &b = rd.b;
+    const u32 r = rd.r;
+    const u32 flags = rd.flags;
+    const i32 isize = b.isize[r];
+    // hasWellDefinedFragmentSize (:117-146)
+    if (isize == 0) return;
+    if (!(flags & F_PAIRED)) return;
+    if ((flags & F_UNMAP) || (flags & F_MATE_UNMAP)) return;
+    const bool rev = flags & F_REVERSE, mate_rev = flags & F_MATE_REVERSE;
+    if (rev == mate_rev) return;
+    bool ok = rev ? (b.astop[r] > b.mstart[r]) : (rd.astart <= b.mstart[r] + u32(isize));
+    if (!ok) return;
+    // getAdaptorBoundary (:150-163)
+    u32 boundary;
+    if (rev) boundary = u32(b.mstart[r] - 1);
+    else boundary = u32(rd.astart + u32(isize < 0 ? -isize : isize) + 1u);
+    if (boundary == U32_NONE) return;
+    const us2 rw = ref_window_w(rd, w, 0, lane);
+    if (boundary < rd.astart + u32(rw.x) || boundary > rd.astart + u32(rw.y)) return;
+    if (rev) {
+        // hardClipByReferenceCoordinates with refStart = -1 (:251-266)
+        const int stop = read_coord_for_ref_w(rd, u32(int(boundary)), false, lane);
+        w.x = tmax<u16>(w.x, u16(u16(stop) + 1));
+    } else {
+        int start;
+        if (int(boundary) < 0) start = 0;  // refStart < 0 branch
+        else start = read_coord_for_ref_w(rd, u32(int(boundary)), true, lane);
+        w.y = tmin<u16>(w.y, u16(u16(start) - 1));
+    }
+}
+
+// compute_no_insertions_window (device/cigar.cu:410-471); (0xFFFF, 0xFFFF) when nothing qualifies
+__device__ us2 no_insertions_window_w(const Read &rd, us2 w, int lane) {
+    us2 out = {U16_NONE, U16_NONE};
+    const u32 i = first_from(0, rd.n, lane, [&](u32 e) {
+        const u16 ro = rd.readc(e);
+        return ro != U16_NONE && ro >= w.x && rd.ty[e] != EV_I;
+    });
+    if (i < rd.n) out.x = rd.readc(i);
+    const int k = last_below(int(rd.n), lane, [&](u32 e) {
+        const u16 ro = rd.readc(e);
+        return ro != U16_NONE && ro <= w.y && rd.ty[e] != EV_I;
+    });
+    if (k >= 0) out.y = rd.readc(u32(k));
+    return out;
+}
+
+// compute_error_vectors (device/cigar.cu:616-737) on the warp's staged base flags: the events of an M op
+// lane-strided (each base of an M op belongs to one event), I and D ops as scalars written by lane 0
+__device__ u16 error_vectors_w(const Read &rd, const DevContig *g, us2 w, us2 rw, u8 *sbf, int lane) {
+    const DevBatch &b = rd.b;
+    const bool neg = rd.flags & F_REVERSE;
+    u32 cur = 0, nerr = 0;
+    const u32 c0 = b.cigar_start[rd.r], c1 = c0 + b.cigar_len[rd.r];
+    for (u32 c = c0; c < c1; c++) {
+        const u32 e0 = rd.w.cigar_offsets[c] - rd.cs, e1 = rd.w.cigar_offsets[c + 1] - rd.cs;
+        const u32 op = op_code(b.cigars[c]);
+        if (op == OP_M) {
+            for (u32 base = e0; base < e1; base += 32) {
+                const u32 i = base + u32(lane);
+                bool err = false;
+                if (i < e1) {
+                    const u16 rc = rd.readc(i);
+                    const u8 rbp = rd.sym(rc);
+                    const u8 fbp = contig_at(*g, u64(rd.astart) + rd.refc(i));
+                    if (fbp != rbp) {
+                        sbf[rc] |= BF_SNP;
+                        err = rc >= w.x && rc <= w.y;
+                    }
+                }
+                nerr += __popc(__ballot_sync(WFULL, err));
+            }
+            if (e1 > e0) cur = rd.readc(e1 - 1);
+        } else if (op == OP_I) {
+            cur = rd.readc(e0);
+            if (cur >= w.x && cur <= w.y) {
+                const int off = neg ? int(cur) + int(op_len(b.cigars[c])) : int(cur) - 1;
+                if (off >= 0 && off <= int(w.y)) {
+                    __syncwarp();
+                    if (lane == 0) sbf[off] |= BF_INS;
+                    nerr++;
+                }
+            }
+        } else if (op == OP_D) {
+            const u16 cref = rd.refc(e0);
+            if (cref >= rw.x && cref <= rw.y) {
+                __syncwarp();
+                if (!neg) {
+                    if (lane == 0) sbf[u16(cur)] |= BF_DEL;
+                    nerr++;
+                } else {
+                    const u16 off = u16(cur + 1);
+                    if (off < rd.rlen) {
+                        if (lane == 0) sbf[off] |= BF_DEL;
+                        nerr++;
+                    }
+                }
+            }
+        }
+        __syncwarp();
+    }
+    return u16(nerr);
+}
+
+// compute_vcf_ranges + filter_bps (device/snp_filter.cu:162-395): per overlapping feature the start event by
+// a ballot search, the short walks around it as scalars, the masked bases lane-strided
+__device__ void filter_known_sites_w(const Read &rd, us2 w, us2 rw, u8 *sbf, int lane) {
     const u32 ch = rd.b.chromosome[rd.r];
     if (ch >= rd.ref.num_site_contigs) return;
     const DevSites db = rd.ref.sites[ch];
@@ -417,13 +424,12 @@ __device__ void filter_known_sites(const Read &rd, us2 w, us2 rw, u8 *bf) {
     for (u32 feature = vx; feature <= vy; feature++) {
         const int fstart = int(db.start[feature] - rd.astart);
         const int fend = int(db.stop[feature] - rd.astart);
-        u32 ev;
-        u16 ref_coord = U16_NONE;
-        for (ev = 0; ev < n; ev++) {
-            ref_coord = rd.refc(ev);
-            if (ref_coord != U16_NONE && int(ref_coord) >= fstart) break;
-        }
+        u32 ev = first_from(0, n, lane, [&](u32 e) {
+            const u16 rc = rd.refc(e);
+            return rc != U16_NONE && int(rc) >= fstart;
+        });
         if (ev == n) continue;
+        const u16 ref_coord = rd.refc(ev);
         int left = int(ref_coord) - fstart;
         u32 evs = ev;
         if (left > 0) {
@@ -453,7 +459,8 @@ __device__ void filter_known_sites(const Read &rd, us2 w, us2 rw, u8 *bf) {
         if ((a < w.x && z < w.x) || (a > w.y && z > w.y)) continue;
         a = tmin<u32>(tmax<u32>(a, w.x), w.y);
         z = tmin<u32>(tmax<u32>(z, w.x), w.y);
-        for (u32 d = a; d <= z; d++) bf[d] &= u8(~BF_ACTIVE);
+        for (u32 d = a + u32(lane); d <= z; d += 32) sbf[d] &= u8(~BF_ACTIVE);
+        __syncwarp();
     }
 }
 
@@ -486,86 +493,96 @@ __device__ bool hmm_window(const Read &rd, const DevContig *g, u16 nerr, us2 w, 
     return true;
 }
 
-__global__ void __launch_bounds__(128) k_prep(DevBatch b, DevRef ref, BatchWork w) {
-    const u32 r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= b.R) return;
-    u8 status = RS_FILTERED;
-    u32 filtered = 0;
-    const u32 qs = b.qual_start[r];
-    const u32 rlen = b.read_len[r];
-    u8 *bf = w.bflags + qs;
+constexpr int PREP_WARPS = 8;
 
-    // filter_invalid_reads -> alignment windows -> filter_malformed_reads (device/pipeline.cu:66-80)
-    bool pass = passes_invalid_filters(b, r);
-    if (pass) {
-        u32 wx, wy, covered;
-        bool bad_op;
-        alignment_window(b, r, wx, wy, covered, bad_op);
-        // filter_if_read_malformed (device/read_filters.cu:77-154); the uint16 contig id never equals
-        // uint32(-1), so those checks are inert. Unknown contigs fail the contig-end check; reads whose
-        // CIGAR does not cover read_len bases or holds an op code above X are rejected (undefined in the
-        // reference).
-        const u32 ch = b.chromosome[r];
-        const DevContig *g = contig_of(ref, ch);
-        if (!(b.flags[r] & F_UNMAP)) {
-            if (b.astart[r] == U32_NONE) pass = false;
-            else if (wy <= wx) pass = false;
-            else if (wx >= (g ? g->size : 0)) pass = false;
-            else if (b.cigar_len[r] == 0) pass = false;
+// K1: one warp per read. Filters and CIGAR-op walks run as identical scalars on every lane; event scans are
+// ballots and per-event / per-base work is lane-strided; the read's base flags live in shared memory until
+// written out once.
+__global__ void __launch_bounds__(PREP_WARPS * 32) k_prep(DevBatch b, DevRef ref, BatchWork w) {
+    __shared__ u8 s_bf[PREP_WARPS][512];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    u8 *sbf = s_bf[wib];
+    for (u32 r = blockIdx.x * PREP_WARPS + wib; r < b.R; r += gridDim.x * PREP_WARPS) {
+        const u32 qs = b.qual_start[r];
+        const u32 rlen = b.read_len[r];
+
+        // filter_invalid_reads -> alignment windows -> filter_malformed_reads (device/pipeline.cu:66-80)
+        bool pass = passes_invalid_filters(b, r);
+        if (pass) {
+            u32 wx, wy, covered;
+            bool bad_op;
+            alignment_window(b, r, wx, wy, covered, bad_op);
+            // filter_if_read_malformed (device/read_filters.cu:77-154); the uint16 contig id never equals
+            // uint32(-1), so those checks are inert. Unknown contigs fail the contig-end check; reads whose
+            // CIGAR does not cover read_len bases or holds an op code above X are rejected (undefined in the
+            // reference).
+            const DevContig *g0 = contig_of(ref, b.chromosome[r]);
+            if (!(b.flags[r] & F_UNMAP)) {
+                if (b.astart[r] == U32_NONE) pass = false;
+                else if (wy <= wx) pass = false;
+                else if (wx >= (g0 ? g0->size : 0)) pass = false;
+                else if (b.cigar_len[r] == 0) pass = false;
+            }
+            if (b.rg[r] == U32_NONE) pass = false;
+            if (b.qual_len[r] != rlen) pass = false;
+            if (rlen == 0) pass = false;
+            if (covered != rlen || bad_op) pass = false;
         }
-        if (b.rg[r] == U32_NONE) pass = false;
-        if (b.qual_len[r] != rlen) pass = false;
-        if (rlen == 0) pass = false;
-        if (covered != rlen || bad_op) pass = false;
-    }
-    if (!pass) {
-        filtered = 1;
-        w.status[r] = RS_FILTERED;
-        atomicAdd(&w.counters[5], filtered);
-        return;
-    }
+        if (!pass) {
+            if (lane == 0) {
+                w.status[r] = RS_FILTERED;
+                atomicAdd(&w.counters[5], 1u);
+            }
+            continue;
+        }
 
-    Read rd(b, ref, w, r);
-    const DevContig *g = contig_of(ref, b.chromosome[r]);
-    expand_read(rd);
+        Read rd(b, ref, w, r);
+        const DevContig *g = contig_of(ref, b.chromosome[r]);
+        expand_read_w(rd, lane);
+        // start_batch: every base active (device/firepony_context.cu:52-59); error bits cleared
+        for (u32 i = u32(lane); i < rlen; i += 32) sbf[i] = BF_ACTIVE;
+        __syncwarp();
 
-    // start_batch: every base active (device/firepony_context.cu:52-59); error bits cleared
-    for (u32 i = 0; i < rlen; i++) bf[i] = BF_ACTIVE;
+        us2 wcl = {0, u16(rlen - 1)};  // read_window_init (device/cigar.cu:97-109)
+        remove_adapters_w(rd, wcl, lane);
+        remove_soft_clips(rd, wcl);
+        const us2 ni = no_insertions_window_w(rd, wcl, lane);
+        const us2 rw = ref_window_w(rd, ni, U16_NONE, lane);
+        const u16 nerr = error_vectors_w(rd, g, wcl, rw, sbf, lane);
 
-    us2 wcl = {0, u16(rlen - 1)};  // read_window_init (device/cigar.cu:97-109)
-    remove_adapters(rd, wcl);
-    remove_soft_clips(rd, wcl);
-    const us2 ni = no_insertions_window(rd, wcl);
-    const us2 rw = reference_window(rd, ni);
-    const u16 nerr = error_vectors(rd, g, wcl, rw, bf);
+        // filter_bases (device/read_filters.cu:375-439)
+        for (u32 i = u32(lane); i < rlen; i += 32) {
+            const u8 bp = rd.sym(i);
+            const bool regular = bp == IUPAC_A || bp == IUPAC_C || bp == IUPAC_G || bp == IUPAC_T;
+            if (!regular || b.quals[qs + i] < 6) sbf[i] &= u8(~BF_ACTIVE);
+        }
+        __syncwarp();
+        filter_known_sites_w(rd, wcl, rw, sbf, lane);
 
-    // filter_bases (device/read_filters.cu:375-439)
-    for (u32 i = 0; i < rlen; i++) {
-        const u8 bp = rd.sym(i);
-        const bool regular = bp == IUPAC_A || bp == IUPAC_C || bp == IUPAC_G || bp == IUPAC_T;
-        if (!regular || b.quals[qs + i] < 6) bf[i] &= u8(~BF_ACTIVE);
-    }
-    filter_known_sites(rd, wcl, rw, bf);
+        ss2 hw;
+        u16 bw = 0;
+        const bool hmm_ok = hmm_window(rd, g, nerr, wcl, ni, rw, hw, bw);
+        const u8 status = hmm_ok ? RS_ACTIVE : RS_REMOVED;
+        if (!hmm_ok) {
+            // the read's events lose their read coordinates (device/baq.cu:136-158): it contributes nothing
+            for (u32 e = u32(lane); e < rd.n; e += 32) rd.rc[e] = u32(U16_NONE) | (rd.rc[e] & 0xFFFF0000u);
+        }
+        for (u32 i = u32(lane); i < rlen; i += 32) w.bflags[qs + i] = sbf[i];
 
-    ss2 hw;
-    u16 bw = 0;
-    const bool hmm_ok = hmm_window(rd, g, nerr, wcl, ni, rw, hw, bw);
-    status = hmm_ok ? RS_ACTIVE : RS_REMOVED;
-    if (!hmm_ok) {
-        // the read's events lose their read coordinates (device/baq.cu:136-158): it contributes nothing
-        for (u32 e = 0; e < rd.n; e++) rd.rc[e] = u32(U16_NONE) | (rd.rc[e] & 0xFFFF0000u);
-    }
-
-    u16 *win = w.win + size_t(r) * 8;
-    win[0] = wcl.x; win[1] = wcl.y; win[2] = ni.x; win[3] = ni.y; win[4] = rw.x; win[5] = rw.y;
-    w.hmm[size_t(r) * 2 + 0] = hw.x;
-    w.hmm[size_t(r) * 2 + 1] = hw.y;
-    w.bw[r] = bw;
-    w.nerr[r] = nerr;
-    w.status[r] = status;
-
-    if (status == RS_ACTIVE) {
-        if (nerr != 0) {
+        if (lane == 0) {
+            u16 *win = w.win + size_t(r) * 8;
+            win[0] = wcl.x; win[1] = wcl.y; win[2] = ni.x; win[3] = ni.y; win[4] = rw.x; win[5] = rw.y;
+            w.hmm[size_t(r) * 2 + 0] = hw.x;
+            w.hmm[size_t(r) * 2 + 1] = hw.y;
+            w.bw[r] = bw;
+            w.nerr[r] = nerr;
+            w.status[r] = status;
+        }
+        if (status == RS_ACTIVE && nerr == 0) {
+            // read_flat_baq (device/baq.cu:842-868)
+            for (u32 i = wcl.x + u32(lane); i <= wcl.y; i += 32) w.tag[qs + i] = NO_BAQ_UNCERTAINTY;
+        }
+        if (lane == 0 && status == RS_ACTIVE && nerr != 0) {
             // BAQ work list by band class: 0 -> bw <= 7, 1 -> bw <= 15, 2 -> wider
             const u32 cls = bw <= 7 ? 0 : (bw <= 15 ? 1 : 2);
             const u32 slot = atomicAdd(&w.counters[cls], 1u);
@@ -588,10 +605,8 @@ __global__ void __launch_bounds__(128) k_prep(DevBatch b, DevRef ref, BatchWork 
             atomicAdd(&w.counters[6], 1u);
             atomicMax(&w.counters[7], u32(wcl.y - wcl.x + 1));
             atomicMax(&w.counters[12 + cls], u32(bw));
-        } else {
-            // read_flat_baq (device/baq.cu:842-868)
-            for (u32 i = wcl.x; i <= wcl.y; i++) w.tag[qs + i] = NO_BAQ_UNCERTAINTY;
         }
+        __syncwarp();
     }
 }
 
@@ -760,7 +775,9 @@ void launch_op_lengths(const DevBatch &b, u32 *out, cudaStream_t s) {
 
 void launch_prep(const DevBatch &b, const DevRef &ref, const BatchWork &w, cudaStream_t s) {
     if (!b.R) return;
-    k_prep<<<(b.R + 127) / 128, 128, 0, s>>>(b, ref, w);
+    u32 blocks = (b.R + PREP_WARPS - 1) / PREP_WARPS;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_prep<<<blocks, PREP_WARPS * 32, 0, s>>>(b, ref, w);
     g_kernel_launches++;
 }
 
