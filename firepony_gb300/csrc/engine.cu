@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -101,7 +102,14 @@ struct fp_engine {
     u64 staged_bases = 0;  // bases counted into the u32 stage since the last merge
 
     // batch buffers
-    DevBuf in_buf;
+    // two device input buffers: a batch prefetched on the copy stream fills one while the other is in use
+    DevBuf in_bufs[2];
+    int in_state[2] = {0, 0};  // 0 free, 1 holds a prefetched batch, 2 in use by a submit
+    const void *in_src[2][17] = {};
+    uint64_t in_counts[2][4] = {};
+    cudaEvent_t in_ev[2] = {nullptr, nullptr};
+    cudaStream_t st_copy = nullptr;
+    std::mutex in_mu;
     DevBatch batch{};
     DevBuf oplen, cigoff, ev_rc, ev_type, per_read, per_base, lists, counters, entry_cnt, entry_off;
     DevBuf entries, entries_alt, sort_tmp, scan_tmp, s32, s32b, s64;
@@ -204,6 +212,9 @@ fp_status fp_engine_create(const fp_options *o, fp_engine **out) {
         cudaDeviceGetStreamPriorityRange(&least, &greatest);
         e = cudaStreamCreateWithPriority(&eng->st2, cudaStreamNonBlocking, greatest);
     }
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&eng->st_copy, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&eng->in_ev[0], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&eng->in_ev[1], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&eng->fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&eng->join, cudaEventDisableTiming);
     if (e != cudaSuccess) {
@@ -248,9 +259,10 @@ void fp_engine_destroy(fp_engine *eng) {
     cudaSetDevice(eng->device);
     if (eng->st) cudaStreamSynchronize(eng->st);
     if (eng->st2) cudaStreamSynchronize(eng->st2);
+    if (eng->st_copy) cudaStreamSynchronize(eng->st_copy);
     for (auto &b : eng->contig_bufs) b.release();
     for (auto &b : eng->site_bufs) b.release();
-    DevBuf *bufs[] = {&eng->d_contigs, &eng->d_sites, &eng->tab_obs, &eng->tab_mism, &eng->tab_stage, &eng->tab_cyc, &eng->in_buf, &eng->oplen,
+    DevBuf *bufs[] = {&eng->d_contigs, &eng->d_sites, &eng->tab_obs, &eng->tab_mism, &eng->tab_stage, &eng->tab_cyc, &eng->in_bufs[0], &eng->in_bufs[1], &eng->oplen,
                       &eng->cigoff, &eng->ev_rc, &eng->ev_type, &eng->per_read, &eng->per_base, &eng->lists,
                       &eng->counters, &eng->entry_cnt, &eng->entry_off, &eng->entries, &eng->entries_alt,
                       &eng->sort_tmp, &eng->scan_tmp, &eng->s32, &eng->s32b, &eng->s64};
@@ -260,6 +272,9 @@ void fp_engine_destroy(fp_engine *eng) {
     if (eng->fork) cudaEventDestroy(eng->fork);
     if (eng->join) cudaEventDestroy(eng->join);
     if (eng->st2) cudaStreamDestroy(eng->st2);
+    if (eng->st_copy) cudaStreamDestroy(eng->st_copy);
+    for (auto &x : eng->in_ev)
+        if (x) cudaEventDestroy(x);
     if (eng->st) cudaStreamDestroy(eng->st);
     delete eng;
 }
@@ -317,6 +332,68 @@ fp_status fp_engine_set_known_sites(fp_engine *eng, uint32_t id, const uint32_t 
     return upload_refs(eng);
 }
 
+// ---- batch inputs: the 17 host arrays of a view, their byte sizes and offsets in a device input buffer ----
+struct ViewArrays {
+    const void *src[17];
+    size_t size[17];
+    size_t off[17];
+    size_t total;
+};
+static ViewArrays view_arrays(const fp_batch_view *v) {
+    ViewArrays a;
+    const uint64_t R = v->num_reads, Q = v->num_qualities, C = v->num_cigar_ops, W = (v->num_read_symbols + 7) / 8;
+    const void *src[] = {v->chromosome, v->alignment_start, v->alignment_stop, v->mate_alignment_start,
+                         v->inferred_insert_size, v->cigars, v->cigar_start, v->cigar_len, v->reads,
+                         v->read_start, v->read_len, v->qualities, v->qual_start, v->qual_len, v->flags, v->mapq,
+                         v->read_group};
+    const size_t size[] = {R * 2, R * 4, R * 4, R * 4, R * 4, C * 4, R * 4, R * 4, W * 4,
+                           R * 4, R * 4, Q, R * 4, R * 4, R * 2, R * 1, R * 4};
+    a.total = 0;
+    for (int i = 0; i < 17; i++) {
+        a.src[i] = src[i];
+        a.size[i] = size[i];
+        a.off[i] = a.total;
+        a.total += al(size[i] ? size[i] : 1);
+    }
+    return a;
+}
+static bool same_view(const fp_engine *eng, int k, const fp_batch_view *v, const ViewArrays &a) {
+    const uint64_t counts[4] = {v->num_reads, v->num_cigar_ops, v->num_read_symbols, v->num_qualities};
+    for (int i = 0; i < 4; i++)
+        if (eng->in_counts[k][i] != counts[i]) return false;
+    for (int i = 0; i < 17; i++)
+        if (eng->in_src[k][i] != a.src[i]) return false;
+    return true;
+}
+// queues the H2D copies of a view into input buffer k on stream s
+static fp_status stage_inputs(fp_engine *eng, int k, const fp_batch_view *v, const ViewArrays &a, cudaStream_t s) {
+    CK(eng->in_bufs[k].ensure(a.total), "batch input allocation");
+    char *base = eng->in_bufs[k].as<char>();
+    for (int i = 0; i < 17; i++)
+        if (a.size[i]) CK(cudaMemcpyAsync(base + a.off[i], a.src[i], a.size[i], cudaMemcpyHostToDevice, s), "H2D");
+    const uint64_t counts[4] = {v->num_reads, v->num_cigar_ops, v->num_read_symbols, v->num_qualities};
+    for (int i = 0; i < 4; i++) eng->in_counts[k][i] = counts[i];
+    for (int i = 0; i < 17; i++) eng->in_src[k][i] = a.src[i];
+    return FP_OK;
+}
+
+fp_status fp_engine_prefetch_batch(fp_engine *eng, const fp_batch_view *v) {
+    if (!eng || !v) return FP_BAD_INPUT;
+    if (v->num_reads == 0) return FP_OK;
+    const ViewArrays a = view_arrays(v);
+    for (int i = 0; i < 17; i++)
+        if (!a.src[i] && a.size[i]) return eng->fail(FP_BAD_INPUT, "null batch array");
+    CK(cudaSetDevice(eng->device), "set device");
+    std::lock_guard<std::mutex> lock(eng->in_mu);
+    int k = eng->in_state[0] == 0 ? 0 : (eng->in_state[1] == 0 ? 1 : -1);
+    if (k < 0) return eng->fail(FP_BAD_INPUT, "both input buffers hold batches not yet submitted");
+    const fp_status s = stage_inputs(eng, k, v, a, eng->st_copy);
+    if (s != FP_OK) return s;
+    CK(cudaEventRecord(eng->in_ev[k], eng->st_copy), "prefetch event");
+    eng->in_state[k] = 1;
+    return FP_OK;
+}
+
 static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device);
 
 fp_status fp_engine_submit_batch(fp_engine *eng, const fp_batch_view *v) { return submit(eng, v, false); }
@@ -338,32 +415,55 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
         eng->stats.num_batches++;
         return FP_OK;
     }
-    const void *arrays[] = {v->chromosome, v->alignment_start, v->alignment_stop, v->mate_alignment_start,
-                            v->inferred_insert_size, v->cigars, v->cigar_start, v->cigar_len, v->reads,
-                            v->read_start, v->read_len, v->qualities, v->qual_start, v->qual_len, v->flags, v->mapq,
-                            v->read_group};
-    const size_t sizes[] = {R * 2ull, R * 4ull, R * 4ull, R * 4ull, R * 4ull, C * 4ull, R * 4ull, R * 4ull, W * 4,
-                            R * 4ull, R * 4ull, Q, R * 4ull, R * 4ull, R * 2ull, R * 1ull, R * 4ull};
+    (void)W;
+    ViewArrays va = view_arrays(v);
     for (int i = 0; i < 17; i++)
-        if (!arrays[i] && sizes[i]) return eng->fail(FP_BAD_INPUT, "null batch array");
+        if (!va.src[i] && va.size[i]) return eng->fail(FP_BAD_INPUT, "null batch array");
 
     cudaEventRecord(eng->ev[0], st);
-    // ---- inputs ----
-    size_t total = 0;
+    // ---- inputs: a prefetched copy of this view, or copies queued here into a free input buffer ----
     size_t offs[17];
-    for (int i = 0; i < 17; i++) {
-        offs[i] = total;
-        total += al(sizes[i] ? sizes[i] : 1);
-    }
     char *base = nullptr;
+    // marks the input buffer free again however this call returns
+    struct Release {
+        fp_engine *e;
+        int k = -1;
+        ~Release() {
+            if (k >= 0) {
+                cudaStreamSynchronize(e->st);  // (already idle unless the batch failed part-way)
+                std::lock_guard<std::mutex> lock(e->in_mu);
+                e->in_state[k] = 0;
+            }
+        }
+    } release{eng};
     if (on_device) {
         // arrays are device pointers already: address them relative to a null base
-        for (int i = 0; i < 17; i++) offs[i] = size_t(reinterpret_cast<uintptr_t>(arrays[i]));
+        for (int i = 0; i < 17; i++) offs[i] = size_t(reinterpret_cast<uintptr_t>(va.src[i]));
     } else {
-        CK(eng->in_buf.ensure(total), "batch input allocation");
-        base = eng->in_buf.as<char>();
-        for (int i = 0; i < 17; i++)
-            if (sizes[i]) CK(cudaMemcpyAsync(base + offs[i], arrays[i], sizes[i], cudaMemcpyHostToDevice, st), "H2D");
+        int k = -1;
+        bool prefetched = false;
+        {
+            std::lock_guard<std::mutex> lock(eng->in_mu);
+            for (int j = 0; j < 2 && k < 0; j++)
+                if (eng->in_state[j] == 1 && same_view(eng, j, v, va)) { k = j; prefetched = true; }
+            for (int j = 0; j < 2 && k < 0; j++)
+                if (eng->in_state[j] == 0) k = j;
+            if (k < 0) {
+                // both buffers hold other prefetched views: drop the first one
+                CK(cudaEventSynchronize(eng->in_ev[0]), "prefetch");
+                k = 0;
+            }
+            eng->in_state[k] = 2;
+        }
+        release.k = k;
+        if (prefetched) {
+            CK(cudaStreamWaitEvent(st, eng->in_ev[k], 0), "prefetch wait");
+        } else {
+            const fp_status s0 = stage_inputs(eng, k, v, va, st);
+            if (s0 != FP_OK) return s0;
+        }
+        base = eng->in_bufs[k].as<char>();
+        for (int i = 0; i < 17; i++) offs[i] = va.off[i];
     }
     DevBatch &b = eng->batch;
     b.R = R;

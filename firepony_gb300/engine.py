@@ -21,7 +21,7 @@ EXPORTED = [
     "fp_engine_submit_batch", "fp_engine_finalize", "fp_engine_get_table", "fp_engine_write_report",
     "fp_engine_reset", "fp_engine_get_stats", "fp_engine_debug_last_batch", "fp_report_write", "fp_host_alloc",
     "fp_host_free", "fp_engine_submit_batch_device", "fp_engine_cuda_stream", "fp_sort_entries",
-    "fp_sort_entries_static",
+    "fp_sort_entries_static", "fp_engine_prefetch_batch",
 ]
 
 
@@ -59,6 +59,7 @@ def lib():
         L.fp_report_write.argtypes = [C.c_char_p, C.POINTER(FpTableView), C.POINTER(C.c_char_p), C.c_uint32, C.c_int,
                                       C.c_int, C.c_int, C.c_int]
         L.fp_engine_submit_batch_device.argtypes = [C.c_void_p, C.POINTER(FpBatchView)]
+        L.fp_engine_prefetch_batch.argtypes = [C.c_void_p, C.POINTER(FpBatchView)]
         L.fp_engine_cuda_stream.restype = C.c_void_p
         L.fp_engine_cuda_stream.argtypes = [C.c_void_p]
         L.fp_sort_entries.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_int, C.c_void_p]
@@ -160,6 +161,29 @@ class Engine:
 
     def submit_view(self, view: FpBatchView):
         self._check(lib().fp_engine_submit_batch(self.h, C.byref(view)), "submit_batch")
+
+    def prefetch_view(self, view: FpBatchView):
+        """Queues the batch's host-to-device copy (fp_engine_prefetch_batch); submit the same view next."""
+        self._check(lib().fp_engine_prefetch_batch(self.h, C.byref(view)), "prefetch_batch")
+
+    def submit_pipelined(self, batches):
+        """Submits a sequence of batches (objects with `.view(FpBatchView)`, or views whose arrays the caller
+        keeps alive), prefetching each next batch while the current one runs. A batch object is held until
+        its submit returns, so the arrays its view points at stay valid while their copy is queued."""
+        def as_pair(x):
+            return (x, x.view(FpBatchView)) if hasattr(x, "view") else (x, x)
+        it = iter(batches)
+        first = next(it, None)
+        if first is None:
+            return
+        cur = as_pair(first)
+        self.prefetch_view(cur[1])
+        for x in it:
+            nxt = as_pair(x)
+            self.prefetch_view(nxt[1])
+            self.submit_view(cur[1])
+            cur = nxt
+        self.submit_view(cur[1])
 
     def submit_device_view(self, view: FpBatchView):
         """Submits a batch whose arrays are device pointers (already resident in HBM)."""

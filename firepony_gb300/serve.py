@@ -5,7 +5,8 @@ streams the job's batches through its pipelines and writes the report. A service
 keeps that state resident instead. `JobServer` holds `slots` engines (`fp_engine`), each with the
 reference contigs and known sites uploaded once, and a worker thread per engine that takes jobs from one
 FIFO queue: `fp_engine_reset` (tables to zero, residency kept), the job's batches through
-`fp_engine_submit_batch` (host buffers, copies included), `fp_engine_finalize`. Engines run on their own
+`fp_engine_submit_batch` (host buffers, copies included; each next batch's copy is queued with
+`fp_engine_prefetch_batch` while the current one runs), `fp_engine_finalize`. Engines run on their own
 CUDA streams, so two jobs share the GPU when more than one is in flight. A job's latency is the time from
 its arrival (submission) to its finished tables.
 
@@ -86,8 +87,8 @@ class JobServer:
             start = time.perf_counter()
             try:
                 eng.reset()
-                for b in job.batches():
-                    eng.submit(b)
+                # each next batch's copy is queued while the current one runs
+                eng.submit_pipelined(job.batches())
                 tables = eng.finalize()
                 p.result = JobResult(job.job_id, job.num_reads, job.arrival, start, time.perf_counter(),
                                      tables if self.keep_tables else None)

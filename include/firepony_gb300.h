@@ -160,6 +160,15 @@ fp_status fp_engine_set_known_sites(fp_engine *engine, uint32_t contig_id, const
  * device/pipeline.cu:56-147). Returns once the host buffers may be reused. */
 fp_status fp_engine_submit_batch(fp_engine *engine, const fp_batch_view *batch);
 
+/* Queues the host-to-device copy of a batch on the engine's copy stream and returns at once (no reference
+ * counterpart: the reference downloads a batch synchronously, device/pipeline_interface.cu:206-220). A
+ * following fp_engine_submit_batch with the same view (same pointers and counts) uses the copy instead of
+ * copying again, so the copy of batch n+1 overlaps the processing of batch n:
+ *     prefetch(b0); for each i: prefetch(b[i+1]); submit(b[i]);
+ * The host buffers must stay unchanged until that submit returns; page-locked buffers (fp_host_alloc) make
+ * the copy asynchronous. Two batches can be prefetched ahead of their submits. */
+fp_status fp_engine_prefetch_batch(fp_engine *engine, const fp_batch_view *batch);
+
 /* Same as fp_engine_submit_batch for a batch whose arrays are already in device memory (device pointers,
  * same layout). For data kept resident on the GPU (serving, benchmarking the kernels alone). */
 fp_status fp_engine_submit_batch_device(fp_engine *engine, const fp_batch_view *device_batch);

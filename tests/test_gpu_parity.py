@@ -228,3 +228,35 @@ def test_replay_all_edge_cases(native):
     to, so, go = run_oracle(contigs, [batch], n_rg, sites)
     assert_stages_equal(batch, ge, go)
     assert_tables_equal(te, to)
+
+
+def test_prefetched_submits(native):
+    """Batches whose copies were queued ahead (fp_engine_prefetch_batch) give the same tables; a view that was
+    not prefetched, a prefetch that is never submitted and a third prefetch ahead are handled."""
+    from firepony_gb300.engine import Engine, EngineError, PinnedBatch
+    from firepony_gb300.abi import FpBatchView
+    p, ref, batches = make_dataset("precision_20M_151bp_pe", 6000, 1500, 400_000)
+    pinned = [PinnedBatch(b) for b in batches]
+    try:
+        e = Engine(num_read_groups=p.num_read_groups)
+        e.load_reference(ref)
+        e.submit_pipelined([pb.batch for pb in pinned])
+        t1 = e.finalize()
+        e.reset()
+        e.prefetch_view(pinned[3].view)           # submitted last, after other batches
+        e.submit_view(pinned[0].view)             # not prefetched: copied into the other buffer
+        e.prefetch_view(pinned[1].view)
+        with pytest.raises(EngineError):
+            e.prefetch_view(pinned[2].view)       # both input buffers hold unsubmitted batches
+        e.submit_view(pinned[1].view)
+        e.submit_view(pinned[2].view)             # not prefetched
+        e.submit_view(pinned[3].view)             # the copy queued first
+        t2 = e.finalize()
+        e.close()
+    finally:
+        for pb in pinned:
+            pb.close()
+    to, _, _ = run_oracle(ref, batches, p.num_read_groups)
+    assert_tables_equal(t1, to)
+    assert_tables_equal(t2, to)
+    assert FpBatchView is not None
