@@ -32,7 +32,8 @@ constexpr int MIN_BASE_QUAL = 4;
 constexpr u8 NO_BAQ_UNCERTAINTY = 64;      // device/baq.h:38
 
 // read status values (fp_engine_debug_last_batch)
-enum { RS_FILTERED = 0, RS_ACTIVE = 1, RS_REMOVED = 2 };
+// RS_DEFERRED: active, its BAQ result waits for the exact replay (counted by the second covariate pass)
+enum { RS_FILTERED = 0, RS_ACTIVE = 1, RS_REMOVED = 2, RS_DEFERRED = 3 };
 
 // per-base flag bits
 enum { BF_SNP = 1, BF_INS = 2, BF_DEL = 4, BF_ACTIVE = 8 };

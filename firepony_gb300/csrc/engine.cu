@@ -83,7 +83,8 @@ struct fp_engine {
     uint32_t n_rg = 1;
     cudaStream_t st = nullptr;
     cudaStream_t st2 = nullptr;          // band-class-1 BAQ, concurrent with class 0
-    cudaEvent_t fork = nullptr, join = nullptr;
+    cudaStream_t st3 = nullptr;          // first covariate count pass, concurrent with the FP64 replays
+    cudaEvent_t fork = nullptr, join = nullptr, cov1_done = nullptr;
     std::string err;
     bool finalized = false;
 
@@ -213,6 +214,8 @@ fp_status fp_engine_create(const fp_options *o, fp_engine **out) {
         e = cudaStreamCreateWithPriority(&eng->st2, cudaStreamNonBlocking, greatest);
     }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&eng->st_copy, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&eng->st3, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&eng->cov1_done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&eng->in_ev[0], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&eng->in_ev[1], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&eng->fork, cudaEventDisableTiming);
@@ -260,6 +263,7 @@ void fp_engine_destroy(fp_engine *eng) {
     if (eng->st) cudaStreamSynchronize(eng->st);
     if (eng->st2) cudaStreamSynchronize(eng->st2);
     if (eng->st_copy) cudaStreamSynchronize(eng->st_copy);
+    if (eng->st3) cudaStreamSynchronize(eng->st3);
     for (auto &b : eng->contig_bufs) b.release();
     for (auto &b : eng->site_bufs) b.release();
     DevBuf *bufs[] = {&eng->d_contigs, &eng->d_sites, &eng->tab_obs, &eng->tab_mism, &eng->tab_stage, &eng->tab_cyc, &eng->in_bufs[0], &eng->in_bufs[1], &eng->oplen,
@@ -273,6 +277,8 @@ void fp_engine_destroy(fp_engine *eng) {
     if (eng->join) cudaEventDestroy(eng->join);
     if (eng->st2) cudaStreamDestroy(eng->st2);
     if (eng->st_copy) cudaStreamDestroy(eng->st_copy);
+    if (eng->st3) cudaStreamDestroy(eng->st3);
+    if (eng->cov1_done) cudaEventDestroy(eng->cov1_done);
     for (auto &x : eng->in_ev)
         if (x) cudaEventDestroy(x);
     if (eng->st) cudaStreamDestroy(eng->st);
@@ -581,7 +587,18 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
         return FP_OK;
     };
     fp_status s;
-    bool timed_main = false, timed_paths = false;
+    bool timed_main = false, timed_paths = false, cov1_overlapped = false;
+    // K3 first count pass (every active read except the deferred ones). Observation counts go to u32 stage
+    // counters; a key gains at most one count per base of the batch, so the stage is merged into the u64 table
+    // before the bases counted since the last merge could reach 2^32
+    auto count_first_pass = [&](cudaStream_t cs) {
+        if (eng->staged_bases + Q > 0xFFFFFFFFull) {
+            launch_merge_stage(eng->tables, cs);
+            eng->staged_bases = 0;
+        }
+        eng->staged_bases += Q;
+        launch_cov_count(b, w, eng->tables, cs);
+    };
     if (eng->baq_mode == FP_BAQ_FP64) {
         for (int c = 0; c < 3; c++) {
             if (c == 0 && n_cls[0]) { cudaEventRecord(eng->ev[10], st); }
@@ -629,6 +646,19 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
             run_fp32(0, st, eng->s32.p, budget, w.counters + 8);
             cudaEventRecord(eng->ev[14], st);
         }
+        // bands wider than 15: thread-per-read FP64
+        if ((s = run_fp64(w.baq_list + 2ull * R, w.counters + 2, n_cls[2], bw_max[2])) != FP_OK) return s;
+        // every certified read now has its final BQ tags; the reads left for the replay are marked deferred.
+        // The first covariate count pass runs on its own stream beside the replays (with the test hook every
+        // read is replayed, so the pass waits for the whole BAQ stage instead)
+        if (!replay_all) {
+            cudaEventRecord(eng->ev[9], st);
+            CK(cudaStreamWaitEvent(eng->st3, eng->ev[9], 0), "fork");
+            if (split) CK(cudaStreamWaitEvent(eng->st3, eng->ev[12], 0), "fork");
+            count_first_pass(eng->st3);
+            CK(cudaEventRecord(eng->cov1_done, eng->st3), "join");
+            cov1_overlapped = true;
+        }
         if (split) {
             // FP64 replays slow to a crawl beside the FP32 kernel (they share its pipes): the class-1 replay
             // waits for it and then runs beside the class-0 replay
@@ -643,20 +673,18 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
         }
         timed_paths = split && n_cls[0];
         if (split) CK(cudaStreamWaitEvent(st, eng->join, 0), "join");
-        if ((s = run_fp64(w.baq_list + 2ull * R, w.counters + 2, n_cls[2], bw_max[2])) != FP_OK) return s;
     }
     CK(cudaGetLastError(), "BAQ launch");
     cudaEventRecord(eng->ev[4], st);
 
-    // ---- K3 count + scan ----
-    // observation counts go to u32 stage counters; a key gains at most one count per base of the batch, so the
-    // stage is merged into the u64 table before the bases counted since the last merge could reach 2^32
-    if (eng->staged_bases + Q > 0xFFFFFFFFull) {
-        launch_merge_stage(eng->tables, st);
-        eng->staged_bases = 0;
+    // ---- K3 count (second pass: the replayed reads) + scan ----
+    if (cov1_overlapped) CK(cudaStreamWaitEvent(st, eng->cov1_done, 0), "join");
+    else count_first_pass(st);
+    if (eng->baq_mode != FP_BAQ_FP64) {
+        for (int c = 0; c < 2; c++)
+            launch_cov_count_list(b, w, eng->tables, w.esc_list + size_t(c) * R, w.counters + (c ? 10 : 4), n_cls[c],
+                                  st);
     }
-    eng->staged_bases += Q;
-    launch_cov_count(b, w, eng->tables, st);
     launch_cycle_pairs(eng->tables, st);
     launch_exclusive_scan(w.entry_count, w.entry_offset, R, eng->scan_tmp.p, st);
     u32 tail[2];

@@ -141,8 +141,12 @@ __host__ __device__ constexpr u32 hist_words(u32 n_rg) { return n_rg <= HIST_MAX
 
 // One warp per read. Lanes stage the read's qualities, flags, BQ tags and bases in shared memory, then walk
 // the read's CIGAR events 32 at a time (lane = event).
-template <bool EMIT>
-__global__ void __launch_bounds__(COV_WARPS * 32) k_cov(DevBatch b, BatchWork w, Tables t) {
+// Count passes: the first (LIST false) takes every active read and skips the deferred ones; the second
+// (LIST true) takes the reads of a replay list and marks them active again. The emit pass takes every
+// active read.
+template <bool EMIT, bool LIST = false>
+__global__ void __launch_bounds__(COV_WARPS * 32) k_cov(DevBatch b, BatchWork w, Tables t, const u32 *list,
+                                                        const u32 *list_count) {
     __shared__ CovSmem smem[COV_WARPS];
     __shared__ FracSmem fsmem[EMIT ? 1 : COV_WARPS];
     extern __shared__ u32 hist[];
@@ -157,11 +161,16 @@ __global__ void __launch_bounds__(COV_WARPS * 32) k_cov(DevBatch b, BatchWork w,
         for (u32 i = threadIdx.x; i < hw_n; i += blockDim.x) hist[i] = 0;
         __syncthreads();
     }
-    for (u32 r = blockIdx.x * COV_WARPS + warp; r < b.R; r += gridDim.x * COV_WARPS) {
-        if (w.status[r] != RS_ACTIVE) {
-            if (!EMIT && lane == 0) w.entry_count[r] = 0;
+    const u32 n_items = LIST ? *list_count : b.R;
+    for (u32 item = blockIdx.x * COV_WARPS + warp; item < n_items; item += gridDim.x * COV_WARPS) {
+        const u32 r = LIST ? list[item] : item;
+        const u8 status = w.status[r];
+        if (!LIST && status != RS_ACTIVE) {
+            // deferred reads are counted by the second pass, which also writes their entry counts
+            if (!EMIT && lane == 0 && status != RS_DEFERRED) w.entry_count[r] = 0;
             continue;
         }
+        if (LIST && lane == 0) w.status[r] = RS_ACTIVE;
         const u16 *win = w.win + size_t(r) * 8;
         const us2 cw = {win[0], win[1]};
         const u32 qs = b.qual_start[r], rs = b.read_start[r], rlen = b.read_len[r];
@@ -407,8 +416,19 @@ void launch_cov_count(const DevBatch &b, const BatchWork &w, const Tables &t, cu
     u32 blocks = (b.R + COV_WARPS - 1) / COV_WARPS;
     if (blocks > 152 * 16) blocks = 152 * 16;
     const size_t smem = size_t(hist_words(t.ks.n_rg)) * sizeof(u32);
-    if (smem) cudaFuncSetAttribute(k_cov<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    k_cov<false><<<blocks, COV_WARPS * 32, smem, s>>>(b, w, t);
+    if (smem) cudaFuncSetAttribute(k_cov<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    k_cov<false, false><<<blocks, COV_WARPS * 32, smem, s>>>(b, w, t, nullptr, nullptr);
+    g_kernel_launches++;
+}
+
+void launch_cov_count_list(const DevBatch &b, const BatchWork &w, const Tables &t, const u32 *list,
+                           const u32 *count, u32 max_items, cudaStream_t s) {
+    if (!max_items) return;
+    u32 blocks = (max_items + COV_WARPS - 1) / COV_WARPS;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    const size_t smem = size_t(hist_words(t.ks.n_rg)) * sizeof(u32);
+    if (smem) cudaFuncSetAttribute(k_cov<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    k_cov<false, true><<<blocks, COV_WARPS * 32, smem, s>>>(b, w, t, list, count);
     g_kernel_launches++;
 }
 
@@ -422,7 +442,7 @@ void launch_cov_emit(const DevBatch &b, const BatchWork &w, const Tables &t, cud
     if (!b.R) return;
     u32 blocks = (b.R + COV_WARPS - 1) / COV_WARPS;
     if (blocks > 152 * 16) blocks = 152 * 16;
-    k_cov<true><<<blocks, COV_WARPS * 32, 0, s>>>(b, w, t);
+    k_cov<true, false><<<blocks, COV_WARPS * 32, 0, s>>>(b, w, t, nullptr, nullptr);
     g_kernel_launches++;
 }
 

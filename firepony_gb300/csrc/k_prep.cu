@@ -711,6 +711,7 @@ __global__ void __launch_bounds__(64) k_cap(DevBatch b, BatchWork w, const u32 *
                 const u32 cls = w.bw[r] <= 7 ? 0 : 1;
                 const u32 slot = atomicAdd(&w.counters[cls ? 10 : 4], 1u);
                 w.esc_list[size_t(cls) * b.R + slot] = r;
+                w.status[r] = RS_DEFERRED;
             }
             // escalation cause: some MAP state undecided, or only qualities undecided
             const bool st = __any_sync(FULL, by_state);

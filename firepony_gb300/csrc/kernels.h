@@ -97,6 +97,9 @@ void launch_baq_tpr(const DevBatch &b, const DevRef &ref, const BatchWork &w, co
 
 // k_covariates.cu
 void launch_cov_count(const DevBatch &b, const BatchWork &w, const Tables &t, cudaStream_t s);
+// second count pass over a replay list (reads left deferred by the first pass)
+void launch_cov_count_list(const DevBatch &b, const BatchWork &w, const Tables &t, const u32 *list,
+                           const u32 *count, u32 max_items, cudaStream_t s);
 void launch_cov_emit(const DevBatch &b, const BatchWork &w, const Tables &t, cudaStream_t s);
 
 // k_sort.cu
