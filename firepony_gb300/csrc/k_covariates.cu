@@ -91,11 +91,15 @@ __device__ void fractional_errors_warp(const CovSmem &sm, FracSmem &fs, u32 wx, 
                 o[1] = (bfv & BF_INS) ? 1.0f : 0.0f;
                 o[2] = (bfv & BF_DEL) ? 1.0f : 0.0f;
             } else {
+                // float(double(n) / double(len)) as in the reference, computed as one correctly rounded FP32
+                // division: with n <= 2^24 and len < 2^28 the exact quotient is at least 2^-25/len away from any
+                // float rounding midpoint it does not equal, far more than the 2^-53 the double rounding can
+                // move it, so both roundings give the same float
                 const u32 d = fs.pre[hi + 1] - fs.pre[lo];
-                const double len = double(hi - lo + 1);
-                o[0] = float(double(d & 1023u) / len);
-                o[1] = float(double((d >> 10) & 1023u) / len);
-                o[2] = float(double(d >> 20) / len);
+                const float len = float(hi - lo + 1);
+                o[0] = __fdiv_rn(float(d & 1023u), len);
+                o[1] = __fdiv_rn(float((d >> 10) & 1023u), len);
+                o[2] = __fdiv_rn(float(d >> 20), len);
             }
         }
         if (m6) carry_next = c + __ffs(m6) - 1;
