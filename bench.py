@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--replay-rpw", type=int, default=0, help="reads per warp of the FP64 replay kernels (0: default)")
     ap.add_argument("--plain-steps", type=int, default=2, help="batches through the plain FP64 path (0: skip)")
+    ap.add_argument("--engine-flags", type=int, default=0, help="fp_options.flags (FP_FLAG_*) for the timed engine")
     ap.add_argument("--serve-jobs", type=int, default=128, help="jobs of the serving measurement (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="job arrivals per second (Poisson)")
     ap.add_argument("--serve-slots", type=int, default=2, help="engines of the job server")
@@ -221,7 +222,7 @@ def run_gb300(args, rank, world):
     K, W = args.steps, args.warmup
     p, ref, batches = make_workload(K, args.batch_reads)
     eng = Engine(num_read_groups=p.num_read_groups, baq_mode=args.baq, device=rank,
-                 replay_reads_per_warp=args.replay_rpw)
+                 replay_reads_per_warp=args.replay_rpw, flags=args.engine_flags)
     eng.load_reference(ref)
     stream = torch.cuda.ExternalStream(eng.stream)
 
