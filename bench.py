@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--replay-rpw", type=int, default=0, help="reads per warp of the FP64 replay kernels (0: default)")
     ap.add_argument("--plain-steps", type=int, default=2, help="batches through the plain FP64 path (0: skip)")
     ap.add_argument("--engine-flags", type=int, default=0, help="fp_options.flags (FP_FLAG_*) for the timed engine")
+    ap.add_argument("--bam-batches", type=int, default=2, help="workload batches for the BAM input measurement (0: skip)")
     ap.add_argument("--serve-jobs", type=int, default=128, help="jobs of the serving measurement (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="job arrivals per second (Poisson)")
     ap.add_argument("--serve-slots", type=int, default=2, help="engines of the job server")
@@ -172,6 +173,50 @@ def run_serving(args):
             "slots": args.serve_slots, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "mean_ms": float(lat.mean()), "max_ms": float(lat.max()), "reads": reads, "reads_per_s": reads / span,
             "errors": sum(1 for r in res if r.error)}
+
+
+def run_bam(args, res):
+    """BAM input (libfpbam): the first batches of the workload written as a BGZF-compressed BAM file, then
+    (1) decoded alone on all host threads and (2) decoded and recalibrated end to end: BAM file to finished
+    tables, the decode of batch n+1 and its copy overlapping the processing of batch n."""
+    import tempfile
+    from firepony_gb300 import bam
+    from firepony_gb300.engine import Engine
+    try:
+        bam.lib()
+    except RuntimeError as ex:
+        return {"unavailable": str(ex)}
+    batches = res["batches"][:args.bam_batches]
+    ref = res["ref"]
+    p = ref.preset
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "workload.bam")
+        targets = [(f"chr{i}", int(n)) for i, (_, n) in enumerate(ref.contigs)]
+        bam.write_bam(path, targets, [f"rg{i}" for i in range(p.num_read_groups)], batches, level=1)
+        size = os.path.getsize(path)
+        reads = sum(b.num_reads for b in batches)
+        r = bam.BamReader(path)
+        t0 = time.perf_counter()
+        n = sum(b.num_reads for b in r.batches(args.batch_reads))
+        t_dec = time.perf_counter() - t0
+        r.close()
+        eng = Engine(num_read_groups=p.num_read_groups)
+        eng.load_reference(ref)
+        r = bam.BamReader(path)
+        eng.submit_pipelined(r.batches(args.batch_reads))  # warm-up pass
+        eng.finalize()
+        eng.reset()
+        r.close()
+        r = bam.BamReader(path)
+        t0 = time.perf_counter()
+        eng.submit_pipelined(r.batches(args.batch_reads))
+        eng.finalize()
+        t_all = time.perf_counter() - t0
+        r.close()
+        eng.close()
+    return {"reads": reads, "bam_bytes": size, "decode_reads_per_s": n / t_dec, "decode_mb_per_s": size / t_dec / 1e6,
+            "bam_to_tables_reads_per_s": reads / t_all, "host_threads": os.cpu_count(),
+            "note": "BGZF level 1 written from the workload batches; decode = inflate + record conversion"}
 
 
 def cpu_baseline(ref, batches, seconds):
@@ -378,6 +423,7 @@ def main():
             cpu = cpu_baseline(res["ref"], res["batches"], args.cpu_sample_seconds)
         plain = run_plain(args, res) if args.plain_steps > 0 and world == 1 and args.baq == "fp32" else None
         serving = run_serving(args) if args.serve_jobs > 0 and world == 1 else None
+        bam_in = run_bam(args, res) if args.bam_batches > 0 and world == 1 else None
         line = {"metric": METRIC, "value": value, "unit": "reads/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
@@ -391,6 +437,7 @@ def main():
                 "cpu_baseline": cpu,
                 "plain": plain,
                 "serving": serving,
+                "bam": bam_in,
                 "clocks": res["clocks"],
                 "stage_ms": [round(x, 3) for x in res["stage_ms"]],
                 "baq_reads": res["stats"]["baq_reads"],

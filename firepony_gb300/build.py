@@ -87,9 +87,32 @@ def build_synth() -> Path:
     return out
 
 
+CUDA_HOME = Path(NVCC).resolve().parent.parent
+
+
+def zlib_available() -> bool:
+    return any(Path(d, "zlib.h").exists() for d in ("/usr/include", "/usr/local/include"))
+
+
+def build_bam() -> Path | None:
+    """libfpbam.so: BGZF/BAM decoding into the engine's batch layout (include/firepony_gb300_bam.h). Needs
+    zlib; skipped (None) where its header is absent."""
+    if not zlib_available():
+        return None
+    BUILD.mkdir(exist_ok=True)
+    out = BUILD / "libfpbam.so"
+    src = CSRC / "bam.cpp"
+    hdrs = [INCLUDE / "firepony_gb300_bam.h", INCLUDE / "firepony_gb300.h"]
+    if _newer([src] + hdrs, out):
+        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread", "-I", str(INCLUDE),
+              "-I", str(CUDA_HOME / "include"), "-o", str(out), str(src), "-L", str(CUDA_HOME / "lib64"),
+              "-lcudart", "-lz"])
+    return out
+
+
 def build_all(verbose: bool = False) -> None:
-    with cf.ThreadPoolExecutor(max_workers=2) as ex:
-        fs = [ex.submit(build_engine, verbose), ex.submit(build_synth)]
+    with cf.ThreadPoolExecutor(max_workers=3) as ex:
+        fs = [ex.submit(build_engine, verbose), ex.submit(build_synth), ex.submit(build_bam)]
         for f in fs:
             f.result()
 
