@@ -203,13 +203,13 @@ def run_bam(args, res):
         eng = Engine(num_read_groups=p.num_read_groups)
         eng.load_reference(ref)
         r = bam.BamReader(path)
-        eng.submit_pipelined(r.batches(args.batch_reads))  # warm-up pass
+        eng.submit_threaded(r.batches(args.batch_reads))  # warm-up pass
         eng.finalize()
         eng.reset()
         r.close()
         r = bam.BamReader(path)
         t0 = time.perf_counter()
-        eng.submit_pipelined(r.batches(args.batch_reads))
+        eng.submit_threaded(r.batches(args.batch_reads))  # decode on its own thread, overlapping the engine
         eng.finalize()
         t_all = time.perf_counter() - t0
         r.close()

@@ -35,6 +35,15 @@ template <typename F> void parallel_for(int threads, size_t n, F f) {
     for (auto &x : th) x.join();
 }
 
+struct NibbleSwapTable {
+    uint8_t t[256];
+    constexpr NibbleSwapTable() : t() {
+        for (int b = 0; b < 256; b++) t[b] = uint8_t(((b & 15) << 4) | (b >> 4));
+    }
+};
+constexpr NibbleSwapTable kNibbleSwapT{};
+constexpr const uint8_t *kNibbleSwap = kNibbleSwapT.t;
+
 inline uint16_t rd16(const uint8_t *p) { return uint16_t(p[0] | (p[1] << 8)); }
 inline uint32_t rd32(const uint8_t *p) { return uint32_t(p[0]) | (uint32_t(p[1]) << 8) | (uint32_t(p[2]) << 16) | (uint32_t(p[3]) << 24); }
 inline void wr16(std::vector<uint8_t> &v, uint16_t x) { v.push_back(uint8_t(x)); v.push_back(uint8_t(x >> 8)); }
@@ -450,19 +459,20 @@ int64_t fpb_next_batch(fpb_reader *r, uint32_t max_reads, fp_batch_view *v) {
             isize[i] = tlen;
             cstart[i] = cig_off[i];
             clen[i] = n_cig;
-            // 4-bit symbols: BAM holds two per byte, high nibble first; the engine 8 per word, low first
+            // 4-bit symbols: BAM holds two per byte, high nibble first; the engine 8 per word, low first. A
+            // word is four BAM bytes with their nibbles swapped; the last word is zero-padded
             const uint32_t s0 = sym_off[i];
-            const uint32_t words = (l_seq + 7) / 8;
+            const uint32_t nbytes = (l_seq + 1) / 2, words = (l_seq + 7) / 8;
+            uint32_t *dst = reads + s0 / 8;
             for (uint32_t wd = 0; wd < words; wd++) {
                 uint32_t word = 0;
-                for (uint32_t k = 0; k < 8; k++) {
-                    const uint32_t j = wd * 8 + k;
-                    if (j >= l_seq) break;
-                    const uint32_t sym = (seq[j >> 1] >> ((j & 1) ? 0 : 4)) & 0xF;
-                    word |= sym << (4 * k);
+                for (uint32_t k = 0; k < 4; k++) {
+                    const uint32_t j = wd * 4 + k;
+                    if (j < nbytes) word |= uint32_t(kNibbleSwap[seq[j]]) << (8 * k);
                 }
-                reads[s0 / 8 + wd] = word;
+                dst[wd] = word;
             }
+            if (l_seq & 1) dst[(l_seq - 1) / 8] &= ~(0xFu << (4 * (l_seq & 7)));  // odd length: no 2nd nibble
             rstart[i] = s0;
             rlen[i] = l_seq;
             memcpy(quals + qual_off[i], qual, l_seq);

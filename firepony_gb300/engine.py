@@ -166,6 +166,41 @@ class Engine:
         """Queues the batch's host-to-device copy (fp_engine_prefetch_batch); submit the same view next."""
         self._check(lib().fp_engine_prefetch_batch(self.h, C.byref(view)), "prefetch_batch")
 
+    def submit_threaded(self, batches):
+        """submit_pipelined with the batches produced on a separate thread (a decoder): producing batch n+1
+        overlaps the processing of batch n. The producer runs at most one batch ahead of the batch being
+        submitted (what a double-buffered decoder such as the BAM reader allows)."""
+        import queue
+        import threading
+        q = queue.Queue(maxsize=1)
+        done = object()
+        err = []
+
+        def produce():
+            try:
+                for b in batches:
+                    q.put(b)
+            except Exception as ex:  # re-raised on the submitting thread
+                err.append(ex)
+            q.put(done)
+
+        t = threading.Thread(target=produce, daemon=True)
+        t.start()
+
+        def consume():
+            while True:
+                b = q.get()
+                if b is done:
+                    return
+                yield b
+
+        try:
+            self.submit_pipelined(consume())
+        finally:
+            t.join()
+        if err:
+            raise err[0]
+
     def submit_pipelined(self, batches):
         """Submits a sequence of batches (objects with `.view(FpBatchView)`, or views whose arrays the caller
         keeps alive), prefetching each next batch while the current one runs. A batch object is held until

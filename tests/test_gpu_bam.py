@@ -24,12 +24,12 @@ def test_bam_to_tables(native, tmp_path):
     e = Engine(num_read_groups=p.num_read_groups)
     e.load_reference(ref)
     decoded = []
-    # pipelined like a loader thread: batch n+1 is decoded and its copy queued while batch n runs
+    # decoded on a producer thread like a loader: batch n+1 is decoded and its copy queued while batch n runs
     def gen():
         for b in reader.batches(2000):
             decoded.append(b.to_batch())
             yield b
-    e.submit_pipelined(gen())
+    e.submit_threaded(gen())
     tables = e.finalize()
     e.close()
     reader.close()
