@@ -78,6 +78,33 @@ struct PinnedBuf {
     ~PinnedBuf() { release(); }
 };
 
+// growable byte buffer that, unlike std::vector, does not zero new bytes (the streams are filled by fread
+// and inflate right after growing)
+struct ByteBuf {
+    uint8_t *p = nullptr;
+    size_t n = 0, cap = 0;
+    size_t size() const { return n; }
+    uint8_t *data() { return p; }
+    const uint8_t *data() const { return p; }
+    bool resize(size_t m) {
+        if (m > cap) {
+            const size_t c = std::max(m, cap + cap / 2);
+            void *q = realloc(p, c);
+            if (!q) return false;
+            p = static_cast<uint8_t *>(q);
+            cap = c;
+        }
+        n = m;
+        return true;
+    }
+    void erase_prefix(size_t k) {
+        if (k == 0) return;
+        memmove(p, p + k, n - k);
+        n -= k;
+    }
+    ~ByteBuf() { free(p); }
+};
+
 // one set of batch arrays, in fp_batch_view order
 struct BatchBufs {
     PinnedBuf a[17];
@@ -90,9 +117,9 @@ struct fpb_reader {
     int threads = 1;
     std::string err;
     bool eof_in = false;             // no more compressed input
-    std::vector<uint8_t> cbuf;       // compressed bytes not yet inflated
+    ByteBuf cbuf;                    // compressed bytes not yet inflated
     size_t cpos = 0;
-    std::vector<uint8_t> ubuf;       // uncompressed stream not yet decoded
+    ByteBuf ubuf;                    // uncompressed stream not yet decoded
     size_t upos = 0;
     // header
     std::vector<std::string> target_names;
@@ -116,11 +143,11 @@ int fail(fpb_reader *r, const std::string &m) {
 bool read_more(fpb_reader *r, size_t bytes) {
     if (r->eof_in) return false;
     if (r->cpos > 0) {
-        r->cbuf.erase(r->cbuf.begin(), r->cbuf.begin() + long(r->cpos));
+        r->cbuf.erase_prefix(r->cpos);
         r->cpos = 0;
     }
     const size_t old = r->cbuf.size();
-    r->cbuf.resize(old + bytes);
+    if (!r->cbuf.resize(old + bytes)) return false;
     const size_t got = fread(r->cbuf.data() + old, 1, bytes, r->f);
     r->cbuf.resize(old + got);
     if (got < bytes) r->eof_in = true;
@@ -170,11 +197,11 @@ int inflate_blocks(fpb_reader *r, int max_blocks) {
     if (blks.empty()) return 0;
     // compact the decoded stream, then inflate the blocks side by side
     if (r->upos > 0) {
-        r->ubuf.erase(r->ubuf.begin(), r->ubuf.begin() + long(r->upos));
+        r->ubuf.erase_prefix(r->upos);
         r->upos = 0;
     }
     const size_t base = r->ubuf.size();
-    r->ubuf.resize(base + total);
+    if (!r->ubuf.resize(base + total)) return fail(r, "out of memory"), -1;
     std::atomic<int> bad{0};
     parallel_for(r->threads, blks.size(), [&](size_t a, size_t z) {
         z_stream zs;
