@@ -406,17 +406,8 @@ def main():
         dist.init_process_group("nccl")
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     res = run_gb300(args, local_rank, world)
-    import torch
-    ms = res["ms_value"]
-    t_e2e = res["t_e2e"]
-    if world > 1:
-        import torch.distributed as dist
-        x = torch.tensor([ms, t_e2e], device="cuda")
-        dist.all_reduce(x, op=dist.ReduceOp.MAX)
-        ms, t_e2e = float(x[0]), float(x[1])
-    total_reads = res["reads"] * world
-    value = total_reads / (ms / 1e3)
-    e2e = total_reads / t_e2e
+    from firepony_gb300.replicas import job_throughput
+    value, e2e, ms, t_e2e = job_throughput(res["ms_value"], res["t_e2e"], res["reads"], world, device="cuda")
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline and world == 1:
