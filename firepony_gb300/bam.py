@@ -10,6 +10,7 @@ import numpy as np
 from .abi import FpBatchView
 
 _lib = None
+BUFFER_SETS = 3  # FPB_BUFFER_SETS
 
 
 def lib():
@@ -63,7 +64,8 @@ def view_arrays(v: FpBatchView) -> dict:
 
 
 class BamBatch:
-    """A decoded batch: its view (reader-owned memory, valid until the reader's call after next)."""
+    """A decoded batch: its view (reader-owned memory; the reader rotates BUFFER_SETS buffer sets, so the
+    batch stays valid until the call that decodes the batch BUFFER_SETS after it)."""
 
     def __init__(self, view: FpBatchView):
         self._view = view

@@ -128,7 +128,7 @@ struct fpb_reader {
     std::unordered_map<std::string, std::string> rg_name_of_id;  // @RG ID -> name (PU if present, else ID)
     std::unordered_map<std::string, uint32_t> rg_index;         // name -> id, in order of first occurrence
     std::vector<std::string> rg_names;
-    BatchBufs bufs[2];
+    BatchBufs bufs[FPB_BUFFER_SETS];
     int next_set = 0;
 };
 
@@ -442,9 +442,9 @@ int64_t fpb_next_batch(fpb_reader *r, uint32_t max_reads, fp_batch_view *v) {
             }
         }
     }
-    // output arrays (alternating buffer sets)
+    // output arrays (rotating buffer sets)
     BatchBufs &bb = r->bufs[r->next_set];
-    r->next_set ^= 1;
+    r->next_set = (r->next_set + 1) % FPB_BUFFER_SETS;
     const size_t sizes[17] = {n * 2, n * 4, n * 4, n * 4, n * 4, size_t(nc) * 4, n * 4, n * 4, size_t(ns) / 2,
                               n * 4, n * 4, size_t(nq), n * 4, n * 4, n * 2, n, n * 4};
     for (int k = 0; k < 17; k++)

@@ -166,19 +166,34 @@ class Engine:
         """Queues the batch's host-to-device copy (fp_engine_prefetch_batch); submit the same view next."""
         self._check(lib().fp_engine_prefetch_batch(self.h, C.byref(view)), "prefetch_batch")
 
-    def submit_threaded(self, batches):
-        """submit_pipelined with the batches produced on a separate thread (a decoder): producing batch n+1
-        overlaps the processing of batch n. The producer runs at most one batch ahead of the batch being
-        submitted (what a double-buffered decoder such as the BAM reader allows)."""
+    def submit_threaded(self, batches, buffers: int = 3):
+        """submit_pipelined with the batches produced on a separate thread (a decoder): producing batch n+2
+        overlaps the processing of batch n (batch n+1's copy is queued meanwhile). At most `buffers` produced
+        batches are alive at a time: the producer starts batch n+buffers only after batch n's submit has
+        returned, so a decoder that rotates `buffers` buffer sets (the BAM reader) never overwrites a batch
+        whose copy or processing is still pending. Needs buffers >= 2; 3 lets decoding overlap the engine."""
         import queue
         import threading
-        q = queue.Queue(maxsize=1)
+        if buffers < 2:
+            raise ValueError("submit_threaded needs at least two buffers")
+        q = queue.Queue()
+        tokens = threading.Semaphore(buffers)
+        stop = threading.Event()
         done = object()
         err = []
 
         def produce():
             try:
-                for b in batches:
+                it = iter(batches)
+                while True:
+                    while not tokens.acquire(timeout=0.1):
+                        if stop.is_set():
+                            return
+                    if stop.is_set():
+                        return
+                    b = next(it, done)
+                    if b is done:
+                        break
                     q.put(b)
             except Exception as ex:  # re-raised on the submitting thread
                 err.append(ex)
@@ -195,18 +210,25 @@ class Engine:
                 yield b
 
         try:
-            self.submit_pipelined(consume())
+            self.submit_pipelined(consume(), on_submitted=tokens.release)
         finally:
+            stop.set()
             t.join()
         if err:
             raise err[0]
 
-    def submit_pipelined(self, batches):
+    def submit_pipelined(self, batches, on_submitted=None):
         """Submits a sequence of batches (objects with `.view(FpBatchView)`, or views whose arrays the caller
         keeps alive), prefetching each next batch while the current one runs. A batch object is held until
-        its submit returns, so the arrays its view points at stay valid while their copy is queued."""
+        its submit returns, so the arrays its view points at stay valid while their copy is queued.
+        `on_submitted()` is called after each batch's submit has returned (its arrays are no longer read)."""
         def as_pair(x):
             return (x, x.view(FpBatchView)) if hasattr(x, "view") else (x, x)
+
+        def submit(pair):
+            self.submit_view(pair[1])
+            if on_submitted is not None:
+                on_submitted()
         it = iter(batches)
         first = next(it, None)
         if first is None:
@@ -216,9 +238,9 @@ class Engine:
         for x in it:
             nxt = as_pair(x)
             self.prefetch_view(nxt[1])
-            self.submit_view(cur[1])
+            submit(cur)
             cur = nxt
-        self.submit_view(cur[1])
+        submit(cur)
 
     def submit_device_view(self, view: FpBatchView):
         """Submits a batch whose arrays are device pointers (already resident in HBM)."""

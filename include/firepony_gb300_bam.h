@@ -34,8 +34,12 @@ uint32_t fpb_target_length(const fpb_reader *reader, uint32_t index);
 int fpb_set_target_map(fpb_reader *reader, const uint16_t *contig_of_target, uint32_t n);
 
 /* Decodes up to max_reads records into *batch. Returns the number of reads (0 at the end of the file) or a
- * negative value on error. The arrays belong to the reader and stay valid until the call after next (two
- * buffer sets alternate), so a caller may prefetch batch n+1 before submitting batch n. */
+ * negative value on error. The arrays belong to the reader, which rotates FPB_BUFFER_SETS buffer sets: batch n
+ * stays valid until the call that decodes batch n + FPB_BUFFER_SETS starts. A decoder thread may therefore
+ * run ahead of the batch being submitted (n) while batch n+1's copy is queued, as long as it starts batch
+ * n+3 only after batch n's submit has returned. */
+#define FPB_BUFFER_SETS 3
+
 int64_t fpb_next_batch(fpb_reader *reader, uint32_t max_reads, fp_batch_view *batch);
 
 /* Read groups seen so far, in id order (the names the report uses). */

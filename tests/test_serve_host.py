@@ -46,3 +46,83 @@ def test_jobs_cover_requested_reads():
         assert job.num_reads == want
         assert sum(p.num_reads for p in parts) == want
         assert all(p.num_reads <= 500 for p in parts)
+
+
+def test_threaded_submit_never_reuses_a_live_buffer_set():
+    """submit_threaded over a decoder that rotates three buffer sets (as the BAM reader does): every batch is
+    still intact when its copy is queued and when its submit runs, whatever the relative speeds."""
+    import random
+    import threading
+    import time
+    from firepony_gb300.engine import Engine
+
+    sets = [None] * 3
+    lock = threading.Lock()
+    seen = []
+
+    class Decoded:
+        def __init__(self, n):
+            self.n = n
+
+        def view(self, _cls=None):
+            return self
+
+    def decoder(count):
+        for n in range(count):
+            time.sleep(random.uniform(0, 0.003))
+            with lock:
+                sets[n % 3] = n  # overwrites the set of batch n - 3
+            yield Decoded(n)
+
+    class FakeEngine(Engine):
+        def __init__(self):  # no device: only the host-side pipelining is exercised
+            pass
+
+        def prefetch_view(self, v):
+            with lock:
+                assert sets[v.n % 3] == v.n, f"batch {v.n} overwritten before its copy was queued"
+
+        def submit_view(self, v):
+            time.sleep(random.uniform(0, 0.003))
+            with lock:
+                assert sets[v.n % 3] == v.n, f"batch {v.n} overwritten while submitted"
+            seen.append(v.n)
+
+        def __del__(self):
+            pass
+
+    random.seed(3)
+    for count in (0, 1, 2, 3, 7, 40):
+        seen.clear()
+        FakeEngine().submit_threaded(decoder(count), buffers=3)
+        assert seen == list(range(count))
+
+
+def test_threaded_submit_error_does_not_hang():
+    """A failing submit ends submit_threaded with that error; the decoder thread is stopped, not left blocked."""
+    import pytest
+    from firepony_gb300.engine import Engine
+
+    class FailingEngine(Engine):
+        def __init__(self):
+            pass
+
+        def prefetch_view(self, v):
+            pass
+
+        def submit_view(self, v):
+            raise RuntimeError("submit failed")
+
+        def __del__(self):
+            pass
+
+    class B:
+        def view(self, _cls=None):
+            return self
+
+    def endless():
+        while True:
+            yield B()
+
+    with pytest.raises(RuntimeError, match="submit failed"):
+        FailingEngine().submit_threaded(endless(), buffers=3)
