@@ -180,6 +180,7 @@ def run_bam(args, res):
     (1) decoded alone on all host threads and (2) decoded and recalibrated end to end: BAM file to finished
     tables, the decode of batch n+1 and its copy overlapping the processing of batch n."""
     import tempfile
+    import numpy as np
     from firepony_gb300 import bam
     from firepony_gb300.engine import Engine
     try:
@@ -210,13 +211,39 @@ def run_bam(args, res):
         r = bam.BamReader(path)
         t0 = time.perf_counter()
         eng.submit_threaded(r.batches(args.batch_reads))  # decode on its own thread, overlapping the engine
-        eng.finalize()
+        tables_host = eng.finalize()
         t_all = time.perf_counter() - t0
         r.close()
+        eng.reset()
+        # GPU decoding (fpb_next_batch_device): BGZF inflate and record conversion on the device
+        gpu = {}
+        try:
+            r = bam.BamReader(path)
+            eng.submit_threaded(r.batches(args.batch_reads, device=True), device=True)  # warm-up pass
+            eng.finalize()
+            eng.reset()
+            r.close()
+            r = bam.BamReader(path)
+            t0 = time.perf_counter()
+            n_dev = sum(b.num_reads for b in r.batches(args.batch_reads, device=True))
+            t_dec_dev = time.perf_counter() - t0
+            r.close()
+            r = bam.BamReader(path)
+            t0 = time.perf_counter()
+            eng.submit_threaded(r.batches(args.batch_reads, device=True), device=True)
+            tables_dev = eng.finalize()
+            t_all_dev = time.perf_counter() - t0
+            r.close()
+            same = all(np.array_equal(tables_host[t][k], tables_dev[t][k]) for t in tables_host for k in tables_host[t])
+            gpu = {"gpu_decode_reads_per_s": n_dev / t_dec_dev, "gpu_decode_mb_per_s": size / t_dec_dev / 1e6,
+                   "gpu_bam_to_tables_reads_per_s": reads / t_all_dev, "gpu_tables_identical": bool(same)}
+        except RuntimeError as ex:
+            gpu = {"gpu_decode_unavailable": str(ex)}
         eng.close()
     return {"reads": reads, "bam_bytes": size, "decode_reads_per_s": n / t_dec, "decode_mb_per_s": size / t_dec / 1e6,
-            "bam_to_tables_reads_per_s": reads / t_all, "host_threads": os.cpu_count(),
-            "note": "BGZF level 1 written from the workload batches; decode = inflate + record conversion"}
+            "bam_to_tables_reads_per_s": reads / t_all, "host_threads": os.cpu_count(), **gpu,
+            "note": "BGZF level 1 written from the workload batches; decode = inflate + record conversion, on the "
+                    "host threads (decode_*, bam_to_tables_*) or on the GPU (gpu_*); the file is read from the page cache"}
 
 
 def cpu_baseline(ref, batches, seconds):

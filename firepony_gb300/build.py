@@ -101,12 +101,34 @@ def build_bam() -> Path | None:
         return None
     BUILD.mkdir(exist_ok=True)
     out = BUILD / "libfpbam.so"
-    src = CSRC / "bam.cpp"
-    hdrs = [INCLUDE / "firepony_gb300_bam.h", INCLUDE / "firepony_gb300.h"]
-    if _newer([src] + hdrs, out):
-        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread", "-I", str(INCLUDE),
-              "-I", str(CUDA_HOME / "include"), "-o", str(out), str(src), "-L", str(CUDA_HOME / "lib64"),
+    hdrs = [INCLUDE / "firepony_gb300_bam.h", INCLUDE / "firepony_gb300.h", CSRC / "bam_internal.h",
+            CSRC / "bgzf_inflate.cuh"]
+    host_src, host_obj = CSRC / "bam.cpp", BUILD / "bam.cpp.o"
+    gpu_src, gpu_obj = CSRC / "bam_gpu.cu", BUILD / "bam_gpu.cu.o"
+    jobs = []
+    if _newer([host_src] + hdrs, host_obj):
+        jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-pthread", "-I", str(INCLUDE), "-I", str(CSRC),
+                     "-I", str(CUDA_HOME / "include"), "-c", str(host_src), "-o", str(host_obj)])
+    if _newer([gpu_src] + hdrs, gpu_obj):
+        jobs.append([NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-I", str(INCLUDE),
+                     "-I", str(CSRC), "-c", str(gpu_src), "-o", str(gpu_obj)])
+    with cf.ThreadPoolExecutor(max_workers=2) as ex:
+        list(ex.map(_run, jobs))
+    if jobs or _newer([host_obj, gpu_obj], out):
+        _run([NVCC, *ARCH, "-shared", "-o", str(out), str(host_obj), str(gpu_obj), "-Xcompiler", "-pthread",
               "-lcudart", "-lz"])
+    return out
+
+
+def build_inflate_check(sanitize: bool = True) -> Path:
+    """Host build of the BGZF block decoder's unit check (tests/native/inflate_check.cpp) against zlib, with the
+    address and undefined-behaviour sanitizers."""
+    BUILD.mkdir(exist_ok=True)
+    out = BUILD / ("inflate_check_san" if sanitize else "inflate_check")
+    src = ROOT / "tests" / "native" / "inflate_check.cpp"
+    if _newer([src, CSRC / "bgzf_inflate.cuh"], out):
+        san = ["-fsanitize=address,undefined", "-fno-sanitize-recover=undefined", "-g"] if sanitize else []
+        _run(["g++", "-O1", "-std=c++17", *san, "-I", str(CSRC), "-o", str(out), str(src), "-lz"])
     return out
 
 

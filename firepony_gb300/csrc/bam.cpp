@@ -14,7 +14,9 @@
 #include <unordered_map>
 #include <vector>
 
-#include "firepony_gb300_bam.h"
+#include "bam_internal.h"
+
+using namespace fpb_detail;
 
 namespace {
 
@@ -44,93 +46,8 @@ struct NibbleSwapTable {
 constexpr NibbleSwapTable kNibbleSwapT{};
 constexpr const uint8_t *kNibbleSwap = kNibbleSwapT.t;
 
-inline uint16_t rd16(const uint8_t *p) { return uint16_t(p[0] | (p[1] << 8)); }
-inline uint32_t rd32(const uint8_t *p) { return uint32_t(p[0]) | (uint32_t(p[1]) << 8) | (uint32_t(p[2]) << 16) | (uint32_t(p[3]) << 24); }
-inline void wr16(std::vector<uint8_t> &v, uint16_t x) { v.push_back(uint8_t(x)); v.push_back(uint8_t(x >> 8)); }
-inline void wr32(std::vector<uint8_t> &v, uint32_t x) { for (int i = 0; i < 4; i++) v.push_back(uint8_t(x >> (8 * i))); }
-
-// host buffer for batch arrays (grows; contents not kept): page-locked when a CUDA device is present, so
-// the engine's copies run asynchronously; ordinary memory otherwise (decoding needs no GPU)
-struct PinnedBuf {
-    void *p = nullptr;
-    size_t cap = 0;
-    bool pinned = false;
-    void release() {
-        if (p) { if (pinned) cudaFreeHost(p); else free(p); }
-        p = nullptr;
-        cap = 0;
-    }
-    bool ensure(size_t bytes) {
-        if (bytes <= cap && p) return true;
-        release();
-        const size_t want = std::max<size_t>(bytes + bytes / 4, 4096);
-        if (cudaHostAlloc(&p, want, cudaHostAllocDefault) == cudaSuccess) {
-            pinned = true;
-        } else {
-            cudaGetLastError();  // clear the failed allocation's error
-            pinned = false;
-            p = malloc(want);
-            if (!p) return false;
-        }
-        cap = want;
-        return true;
-    }
-    ~PinnedBuf() { release(); }
-};
-
-// growable byte buffer that, unlike std::vector, does not zero new bytes (the streams are filled by fread
-// and inflate right after growing)
-struct ByteBuf {
-    uint8_t *p = nullptr;
-    size_t n = 0, cap = 0;
-    size_t size() const { return n; }
-    uint8_t *data() { return p; }
-    const uint8_t *data() const { return p; }
-    bool resize(size_t m) {
-        if (m > cap) {
-            const size_t c = std::max(m, cap + cap / 2);
-            void *q = realloc(p, c);
-            if (!q) return false;
-            p = static_cast<uint8_t *>(q);
-            cap = c;
-        }
-        n = m;
-        return true;
-    }
-    void erase_prefix(size_t k) {
-        if (k == 0) return;
-        memmove(p, p + k, n - k);
-        n -= k;
-    }
-    ~ByteBuf() { free(p); }
-};
-
-// one set of batch arrays, in fp_batch_view order
-struct BatchBufs {
-    PinnedBuf a[17];
-};
-
 }  // namespace
 
-struct fpb_reader {
-    FILE *f = nullptr;
-    int threads = 1;
-    std::string err;
-    bool eof_in = false;             // no more compressed input
-    ByteBuf cbuf;                    // compressed bytes not yet inflated
-    size_t cpos = 0;
-    ByteBuf ubuf;                    // uncompressed stream not yet decoded
-    size_t upos = 0;
-    // header
-    std::vector<std::string> target_names;
-    std::vector<uint32_t> target_lens;
-    std::vector<uint16_t> contig_of_target;
-    std::unordered_map<std::string, std::string> rg_name_of_id;  // @RG ID -> name (PU if present, else ID)
-    std::unordered_map<std::string, uint32_t> rg_index;         // name -> id, in order of first occurrence
-    std::vector<std::string> rg_names;
-    BatchBufs bufs[FPB_BUFFER_SETS];
-    int next_set = 0;
-};
 
 namespace {
 
@@ -148,7 +65,10 @@ bool read_more(fpb_reader *r, size_t bytes) {
     }
     const size_t old = r->cbuf.size();
     if (!r->cbuf.resize(old + bytes)) return false;
+    const double t0 = now_s();
     const size_t got = fread(r->cbuf.data() + old, 1, bytes, r->f);
+    r->stats.seconds_read += now_s() - t0;
+    r->stats.compressed_bytes += got;
     r->cbuf.resize(old + got);
     if (got < bytes) r->eof_in = true;
     return got > 0;
@@ -229,10 +149,11 @@ int inflate_blocks(fpb_reader *r, int max_blocks) {
     return int(blks.size());
 }
 
-// ensures n undecoded bytes are available; false if the stream ends first
-bool need(fpb_reader *r, size_t n) {
+// ensures n undecoded bytes are available, inflating up to max_blocks blocks at a time; false if the stream
+// ends first
+bool need(fpb_reader *r, size_t n, int max_blocks = 512) {
     while (r->ubuf.size() - r->upos < n) {
-        const int k = inflate_blocks(r, 512);
+        const int k = inflate_blocks(r, max_blocks);
         if (k <= 0) return false;
     }
     return true;
@@ -309,20 +230,21 @@ int fpb_open(const char *path, int threads, fpb_reader **out) {
     r->threads = threads > 0 ? threads : int(std::max(1u, std::thread::hardware_concurrency()));
     r->f = fopen(path, "rb");
     if (!r->f) { delete r; return -1; }
-    // magic, text, targets
-    if (!need(r, 12) || memcmp(r->ubuf.data() + r->upos, "BAM\1", 4) != 0) { fpb_close(r); return -1; }
+    // magic, text, targets: inflated a block at a time, so that the records after the header stay compressed
+    // for whichever decoder (host or GPU) reads them
+    if (!need(r, 12, 1) || memcmp(r->ubuf.data() + r->upos, "BAM\1", 4) != 0) { fpb_close(r); return -1; }
     const uint32_t l_text = rd32(r->ubuf.data() + r->upos + 4);
-    if (!need(r, 12 + size_t(l_text))) { fpb_close(r); return -1; }
+    if (!need(r, 12 + size_t(l_text), 1)) { fpb_close(r); return -1; }
     const std::string text(reinterpret_cast<const char *>(r->ubuf.data() + r->upos + 8), l_text);
     r->upos += 8 + l_text;
     parse_read_groups(r, text);
-    if (!need(r, 4)) { fpb_close(r); return -1; }
+    if (!need(r, 4, 1)) { fpb_close(r); return -1; }
     const uint32_t n_ref = rd32(r->ubuf.data() + r->upos);
     r->upos += 4;
     for (uint32_t i = 0; i < n_ref; i++) {
-        if (!need(r, 4)) { fpb_close(r); return -1; }
+        if (!need(r, 4, 1)) { fpb_close(r); return -1; }
         const uint32_t l_name = rd32(r->ubuf.data() + r->upos);
-        if (!need(r, 8 + size_t(l_name))) { fpb_close(r); return -1; }
+        if (!need(r, 8 + size_t(l_name), 1)) { fpb_close(r); return -1; }
         const char *nm = reinterpret_cast<const char *>(r->ubuf.data() + r->upos + 4);
         r->target_names.emplace_back(nm, strnlen(nm, l_name));
         r->target_lens.push_back(rd32(r->ubuf.data() + r->upos + 4 + l_name));
@@ -335,6 +257,7 @@ int fpb_open(const char *path, int threads, fpb_reader **out) {
 
 void fpb_close(fpb_reader *r) {
     if (!r) return;
+    if (r->dev) destroy_device_decoder(r->dev);
     if (r->f) fclose(r->f);
     delete r;
 }
@@ -357,9 +280,30 @@ const char *fpb_read_group_name(const fpb_reader *r, uint32_t id) {
     return (r && id < r->rg_names.size()) ? r->rg_names[id].c_str() : nullptr;
 }
 
+static int64_t next_batch_host(fpb_reader *r, uint32_t max_reads, fp_batch_view *v);
+
 int64_t fpb_next_batch(fpb_reader *r, uint32_t max_reads, fp_batch_view *v) {
     if (!r || !v) return -1;
+    const double t0 = now_s(), read0 = r->stats.seconds_read;
+    const int64_t n = next_batch_host(r, max_reads, v);
+    r->stats.seconds_decode += (now_s() - t0) - (r->stats.seconds_read - read0);
+    if (n > 0) {
+        r->stats.batches++;
+        r->stats.records += uint64_t(n);
+    }
+    return n;
+}
+
+int fpb_get_stats(const fpb_reader *r, fpb_stats *out) {
+    if (!r || !out) return -1;
+    *out = r->stats;
+    return 0;
+}
+
+static int64_t next_batch_host(fpb_reader *r, uint32_t max_reads, fp_batch_view *v) {
     memset(v, 0, sizeof(*v));
+    if (r->mode == 2) return fail(r, "the reader decodes on the GPU (fpb_next_batch_device)");
+    r->mode = 1;
     // locate the records: length prefixes, in stream order
     std::vector<size_t> rec;
     rec.reserve(max_reads);
@@ -378,6 +322,12 @@ int64_t fpb_next_batch(fpb_reader *r, uint32_t max_reads, fp_batch_view *v) {
             p = r->upos + rel;
         }
         if (bs < 32) return fail(r, "BAM record shorter than its fixed fields");
+        {
+            const uint8_t *b = r->ubuf.data() + p + 4;
+            const uint64_t need_bytes = 32ull + b[8] + 4ull * rd16(b + 12) + (uint64_t(rd32(b + 16)) + 1) / 2 +
+                                        uint64_t(rd32(b + 16));
+            if (need_bytes > bs) return fail(r, "malformed BAM record (its fields exceed its length)");
+        }
         rec.push_back(p - r->upos);
         p += 4 + bs;
     }

@@ -166,12 +166,14 @@ class Engine:
         """Queues the batch's host-to-device copy (fp_engine_prefetch_batch); submit the same view next."""
         self._check(lib().fp_engine_prefetch_batch(self.h, C.byref(view)), "prefetch_batch")
 
-    def submit_threaded(self, batches, buffers: int = 3):
+    def submit_threaded(self, batches, buffers: int = 3, device: bool = False):
         """submit_pipelined with the batches produced on a separate thread (a decoder): producing batch n+2
         overlaps the processing of batch n (batch n+1's copy is queued meanwhile). At most `buffers` produced
         batches are alive at a time: the producer starts batch n+buffers only after batch n's submit has
         returned, so a decoder that rotates `buffers` buffer sets (the BAM reader) never overwrites a batch
-        whose copy or processing is still pending. Needs buffers >= 2; 3 lets decoding overlap the engine."""
+        whose copy or processing is still pending. Needs buffers >= 2; 3 lets decoding overlap the engine.
+        device: the batches' arrays are device pointers (the BAM reader's GPU decoding); each is submitted
+        with fp_engine_submit_batch_device, with no copy."""
         import queue
         import threading
         if buffers < 2:
@@ -210,7 +212,12 @@ class Engine:
                 yield b
 
         try:
-            self.submit_pipelined(consume(), on_submitted=tokens.release)
+            if device:
+                for b in consume():
+                    self.submit_device_view(b.view(FpBatchView))
+                    tokens.release()
+            else:
+                self.submit_pipelined(consume(), on_submitted=tokens.release)
         finally:
             stop.set()
             t.join()

@@ -42,6 +42,31 @@ int fpb_set_target_map(fpb_reader *reader, const uint16_t *contig_of_target, uin
 
 int64_t fpb_next_batch(fpb_reader *reader, uint32_t max_reads, fp_batch_view *batch);
 
+/* Same batches as fpb_next_batch, decoded on the current CUDA device: the compressed BGZF blocks are copied
+ * to the device, inflated there (a thread per block, then a warp per block for the back-references and the
+ * CRC-32 check), the records located and converted by kernels into device arrays. *batch holds DEVICE
+ * pointers for fp_engine_submit_batch_device; the same FPB_BUFFER_SETS rotation applies (batch n stays valid
+ * until the call that decodes batch n + FPB_BUFFER_SETS starts, and by then batch n's submit must have
+ * returned). Returns once the arrays are complete. A reader uses one of fpb_next_batch and
+ * fpb_next_batch_device for all its batches. Replaces the same loader path as fpb_next_batch
+ * (loader/alignments.cu:257-437, io_thread.cu:97-147). */
+int64_t fpb_next_batch_device(fpb_reader *reader, uint32_t max_reads, fp_batch_view *batch);
+
+/* Counters of a reader since fpb_open (no reference counterpart: the reference's loader keeps no statistics). */
+typedef struct fpb_stats {
+    uint64_t batches;            /* non-empty batches returned */
+    uint64_t records;            /* records returned */
+    uint64_t compressed_bytes;   /* BGZF bytes read from the file */
+    uint64_t blocks;             /* BGZF blocks inflated (GPU decoding) */
+    uint64_t extra_rounds;       /* GPU decoding: rounds that gathered more blocks after a stream held too few records */
+    uint64_t serial_walks;       /* GPU decoding: batches whose record starts were found by the one-thread walk */
+    double seconds_read;         /* in file reads */
+    double seconds_decode;       /* in fpb_next_batch / fpb_next_batch_device outside file reads (GPU decoding:
+                                    the host's block parsing and its waits for the device, copies included) */
+} fpb_stats;
+
+int fpb_get_stats(const fpb_reader *reader, fpb_stats *out);
+
 /* Read groups seen so far, in id order (the names the report uses). */
 uint32_t fpb_num_read_groups(const fpb_reader *reader);
 const char *fpb_read_group_name(const fpb_reader *reader, uint32_t id);

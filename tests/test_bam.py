@@ -42,7 +42,9 @@ def test_decode_equals_written(data, max_reads):
     assert r.targets == targets
     got = [b.to_batch() for b in r.batches(max_reads)]
     names = r.read_group_names
+    st = r.stats
     r.close()
+    assert st["records"] == 5000 and st["batches"] == len(got) and st["compressed_bytes"] == path.stat().st_size
     assert sum(b.num_reads for b in got) == 5000
     assert all(b.num_reads <= max_reads for b in got)
     whole = {k: np.concatenate([b[k] for b in batches]) for k in batches[0].arrays}
@@ -75,3 +77,23 @@ def test_target_map_and_bad_file(data, tmp_path):
     bad.write_bytes(b"not a bam file at all")
     with pytest.raises(RuntimeError):
         bam.BamReader(str(bad))
+
+
+def test_bgzf_block_decoder_against_zlib():
+    """The GPU's DEFLATE block decoder (csrc/bgzf_inflate.cuh), built for the host with the address and
+    undefined-behaviour sanitizers: round trips of zlib streams at every level and strategy, CRC-32 and CRC
+    concatenation against zlib, and corrupt or truncated streams that must end in an error status inside
+    the buffers."""
+    import subprocess
+    from firepony_gb300 import build
+    if not build.zlib_available():
+        pytest.skip("zlib headers missing")
+    try:
+        exe = build.build_inflate_check(sanitize=True)
+    except RuntimeError as ex:
+        if "sanitize" not in str(ex) and "asan" not in str(ex):
+            raise
+        exe = build.build_inflate_check(sanitize=False)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.startswith("ok")
