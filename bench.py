@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--replay-rpw", type=int, default=0, help="reads per warp of the FP64 replay kernels (0: default)")
     ap.add_argument("--plain-steps", type=int, default=2, help="batches through the plain FP64 path (0: skip)")
     ap.add_argument("--engine-flags", type=int, default=0, help="fp_options.flags (FP_FLAG_*) for the timed engine")
-    ap.add_argument("--bam-batches", type=int, default=2, help="workload batches for the BAM input measurement (0: skip)")
+    ap.add_argument("--bam-batches", type=int, default=4, help="workload batches for the BAM input measurement (0: skip)")
     ap.add_argument("--serve-jobs", type=int, default=128, help="jobs of the serving measurement (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="job arrivals per second (Poisson)")
     ap.add_argument("--serve-slots", type=int, default=2, help="engines of the job server")

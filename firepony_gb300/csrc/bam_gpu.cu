@@ -776,13 +776,13 @@ bool grow_slab(DeviceDecoder *d, size_t want) {
 
 // Reads the next READ_CHUNK bytes of the file into the slab (growing it by doubling), split into pieces read by
 // parallel pread calls (page-cache copies scale with threads); false at the end of the file or when memory
-// runs out.
-constexpr size_t READ_CHUNK = 64u << 20, READ_PIECE_MIN = 4u << 20;
+// runs out. Chunks are modest so that the unused tail moved to the slab's front at the next batch stays small.
+constexpr size_t READ_CHUNK = 16u << 20, READ_PIECE_MIN = 2u << 20;
 
 bool read_more_dev(fpb_reader *r, DeviceDecoder *d) {
     if (d->file_eof) return false;
     if (d->slab_cap - d->slab_len < READ_CHUNK && !grow_slab(d, d->slab_len + READ_CHUNK)) return false;
-    const size_t want = d->slab_cap - d->slab_len;
+    const size_t want = READ_CHUNK;
     const int np = int(std::max<size_t>(1, std::min<size_t>(size_t(std::max(1, r->threads)), want / READ_PIECE_MIN)));
     const size_t piece = (want + np - 1) / np;
     std::vector<size_t> got(np, 0);

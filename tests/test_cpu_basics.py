@@ -28,6 +28,21 @@ def test_library_exports_every_declared_symbol(native):
     assert not missing, f"missing exports: {missing}"
 
 
+def test_bam_library_exports_every_declared_symbol(native):
+    """libfpbam exports every fpb_ function include/firepony_gb300_bam.h declares."""
+    import ctypes
+    from firepony_gb300 import bam
+    try:
+        lib = bam.lib()
+    except RuntimeError as ex:
+        pytest.skip(str(ex))
+    text = (ROOT / "include" / "firepony_gb300_bam.h").read_text()
+    names = sorted(set(re.findall(r"^\w[\w\s\*]*?\b(fpb_\w+)\s*\(", text, flags=re.M)))
+    assert "fpb_next_batch_device" in names and "fpb_get_stats" in names
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, f"missing exports: {missing}"
+
+
 def test_report_format_small_table(native, tmp_path):
     from firepony_gb300.engine import write_report
     t = {}
