@@ -336,6 +336,13 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
             nqq = QUL(qL - 1);
             nref = REF(qL - 1 - bw > 0 ? qL - 1 - bw : 0);
         }
+        // the MAP step of row i compares with the base's own quality QUL(i - 1): for 1 < i it is nqq (loaded a
+        // row ahead for the next backward step), for row 1 this value (a global load right before its use would
+        // stall the row)
+        const u8 q_first = QUL(0);
+        // the forward scaling factor of the row below (used after that row's backward arithmetic), loaded a row
+        // ahead for the same reason
+        T next_scale = qL >= 2 ? SC(qL - 1) : T(1);
         for (int i = qL; i >= 1; i--) {
             const int beg = 1 > i - bw ? 1 : i - bw;
             const int end = refLen < i + bw ? refLen : i + bw;
@@ -365,7 +372,8 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                     nqq = QUL(i - 1);
                     nref = REF(i - 1 - bw > 0 ? i - 1 - bw : 0);
                 }
-                const T scale_i = SC(i);
+                const T scale_i = next_scale;
+                if (i > 1) next_scale = SC(i - 1);
                 const T y = (i > 1) ? T(1) : T(0);
                 const bool grow = i < bw;  // row i+1 still in the growing band
                 if (!grow) {
@@ -479,7 +487,7 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                 w.baq_state[qi] = u32(max_k);
                 w.baq_amb[qi] = 0;
             } else {
-                const int qo = QUL(i - 1);
+                const int qo = i == 1 ? q_first : nqq;
                 u8 amb = 0;
                 int qv = MIN_BASE_QUAL;
                 u32 state = U32_NONE;
