@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--plain-steps", type=int, default=2, help="batches through the plain FP64 path (0: skip)")
     ap.add_argument("--engine-flags", type=int, default=0, help="fp_options.flags (FP_FLAG_*) for the timed engine")
     ap.add_argument("--bam-batches", type=int, default=4, help="workload batches for the BAM input measurement (0: skip)")
+    ap.add_argument("--batched-batches", type=int, default=96,
+                    help="input batches of the uneven-batch measurement (0: skip)")
+    ap.add_argument("--coalesce-reads", type=int, default=1_000_000, help="fp_options.coalesce_reads of its coalesced run")
     ap.add_argument("--serve-jobs", type=int, default=128, help="jobs of the serving measurement (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="job arrivals per second (Poisson)")
     ap.add_argument("--serve-slots", type=int, default=2, help="engines of the job server")
@@ -136,6 +139,46 @@ def run_plain(args, res):
     reads = n * args.batch_reads
     return {"value": reads / (ms / 1e3), "unit": "reads/s", "baq": "fp64 (every BAQ read exact FP64)",
             "steps": n, "ms_per_step": ms / n}
+
+
+def run_batched(args):
+    """The uneven-batch workload (4 contigs / 100 Mbp, reads of 36-250 bp mixed, 0-8 indels per read, 10% wide
+    deletions, 16 read groups) as a bounded sample of its many small input batches (sizes uniform in 2k-40k
+    reads), from page-locked host buffers through the C ABI: each batch processed alone, then with the engine
+    coalescing them (fp_options.coalesce_reads) into device batches. Wall clock from the first submit to the
+    finished tables; both runs must give identical tables."""
+    import numpy as np
+    from firepony_gb300 import synth
+    from firepony_gb300.engine import Engine, PinnedBatch
+    sizes = synth.uneven_batch_sizes(args.batched_batches, 2000, 40000, seed=2)
+    p = synth.PRESETS["batched_uneven"].scaled(num_reads=int(sizes.sum()))
+    ref = synth.Reference(p)
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+        batches = list(ex.map(lambda i: ref.batch(i, int(sizes[i])), range(len(sizes))))
+    pinned = [PinnedBatch(b) for b in batches]
+    reads = int(sizes.sum())
+    out = {}
+    tables = {}
+    for name, coalesce in (("per_batch", 0), ("coalesced", args.coalesce_reads)):
+        eng = Engine(num_read_groups=p.num_read_groups, coalesce_reads=coalesce)
+        eng.load_reference(ref)
+        eng.submit_pipelined([pb.batch for pb in pinned[:4]])  # warm-up
+        eng.finalize()
+        eng.reset()
+        t0 = time.perf_counter()
+        # (per batch: each batch's copy is prefetched while the previous one runs; coalesced: copied at submit)
+        eng.submit_pipelined([pb.batch for pb in pinned])
+        tables[name] = eng.finalize()
+        dt = time.perf_counter() - t0
+        out[name + "_reads_per_s"] = reads / dt
+        eng.close()
+    same = all(np.array_equal(tables["per_batch"][t][k], tables["coalesced"][t][k])
+               for t in tables["per_batch"] for k in tables["per_batch"][t])
+    return {"workload": "batched_uneven: 4 contigs / 100 Mbp, reads of 36/76/101/151/250 bp, 0-8 indels per read, "
+                        "10% wide deletions, 16 read groups",
+            "batches": len(sizes), "reads": reads, "batch_reads": "uniform 2000-40000", "coalesce_reads": args.coalesce_reads,
+            **out, "speedup": out["coalesced_reads_per_s"] / out["per_batch_reads_per_s"], "tables_identical": bool(same),
+            "inputs": "page-locked host buffers through fp_engine_submit_batch (copies in the timed region)"}
 
 
 def run_serving(args):
@@ -442,6 +485,7 @@ def main():
         plain = run_plain(args, res) if args.plain_steps > 0 and world == 1 and args.baq == "fp32" else None
         serving = run_serving(args) if args.serve_jobs > 0 and world == 1 else None
         bam_in = run_bam(args, res) if args.bam_batches > 0 and world == 1 else None
+        batched = run_batched(args) if args.batched_batches > 0 and world == 1 else None
         line = {"metric": METRIC, "value": value, "unit": "reads/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
@@ -456,6 +500,7 @@ def main():
                 "plain": plain,
                 "serving": serving,
                 "bam": bam_in,
+                "batched": batched,
                 "clocks": res["clocks"],
                 "stage_ms": [round(x, 3) for x in res["stage_ms"]],
                 "baq_reads": res["stats"]["baq_reads"],

@@ -15,7 +15,7 @@ class FpOptions(C.Structure):
     _fields_ = [("device", C.c_int32), ("baq_mode", C.c_int32), ("num_read_groups", C.c_uint32),
                 ("max_batch_reads", C.c_uint32), ("max_batch_bases", C.c_uint64),
                 ("max_batch_cigar_ops", C.c_uint64), ("replay_reads_per_warp", C.c_uint32),
-                ("flags", C.c_uint32)]
+                ("flags", C.c_uint32), ("coalesce_reads", C.c_uint32), ("reserved", C.c_uint32)]
 FP_FLAG_REPLAY_ALL = 1
 
 

@@ -111,9 +111,15 @@ struct fp_engine {
     cudaEvent_t in_ev[2] = {nullptr, nullptr};
     cudaStream_t st_copy = nullptr;
     std::mutex in_mu;
+    // coalescing of small host batches (fp_options.coalesce_reads): a device staging batch of 17 arrays
+    u32 co_target = 0;
+    DevBuf co_buf;
+    size_t co_off[17] = {};
+    u64 co_cap[4] = {};  // capacity: reads, cigar ops, read words, qualities
+    u64 co_n[4] = {};    // staged
     DevBatch batch{};
     DevBuf oplen, cigoff, ev_rc, ev_type, per_read, per_base, lists, counters, entry_cnt, entry_off;
-    DevBuf entries, entries_alt, sort_tmp, scan_tmp, s32, s32b, s64;
+    DevBuf entries, entries_alt, sort_tmp, scan_tmp, s32, s32b, s64, s32w;  // s32w: wide-band exact FP64 scratch
     u64 s64_doubles = 0;
     BatchWork work{};
     uint32_t last_R = 0;
@@ -200,6 +206,7 @@ fp_status fp_engine_create(const fp_options *o, fp_engine **out) {
     if (o->replay_reads_per_warp) eng->replay_rpw = o->replay_reads_per_warp;
     eng->flags = o->flags;
     eng->n_rg = o->num_read_groups;
+    eng->co_target = o->coalesce_reads;
     cudaError_t e = cudaSetDevice(eng->device);
     if (e != cudaSuccess) {
         delete eng;
@@ -234,6 +241,7 @@ fp_status fp_engine_create(const fp_options *o, fp_engine **out) {
     baq64_set_constants(eng->hmm);
     baq_tpr_set_constants(eng->hmm);
     baq_exact_set_constants(eng->hmm);
+    baq_wide_set_constants(eng->hmm);
     EmpConst ec;
     for (int d = 0; d <= 40; d++) ec.prior[d] = log10(gaussian(double(d)));
     for (int bin = 0; bin <= 60; bin++) {
@@ -269,7 +277,7 @@ void fp_engine_destroy(fp_engine *eng) {
     DevBuf *bufs[] = {&eng->d_contigs, &eng->d_sites, &eng->tab_obs, &eng->tab_mism, &eng->tab_stage, &eng->tab_cyc, &eng->in_bufs[0], &eng->in_bufs[1], &eng->oplen,
                       &eng->cigoff, &eng->ev_rc, &eng->ev_type, &eng->per_read, &eng->per_base, &eng->lists,
                       &eng->counters, &eng->entry_cnt, &eng->entry_off, &eng->entries, &eng->entries_alt,
-                      &eng->sort_tmp, &eng->scan_tmp, &eng->s32, &eng->s32b, &eng->s64};
+                      &eng->sort_tmp, &eng->scan_tmp, &eng->s32, &eng->s32b, &eng->s64, &eng->co_buf, &eng->s32w};
     for (DevBuf *b : bufs) b->release();
     for (auto &x : eng->ev)
         if (x) cudaEventDestroy(x);
@@ -386,6 +394,7 @@ static fp_status stage_inputs(fp_engine *eng, int k, const fp_batch_view *v, con
 fp_status fp_engine_prefetch_batch(fp_engine *eng, const fp_batch_view *v) {
     if (!eng || !v) return FP_BAD_INPUT;
     if (v->num_reads == 0) return FP_OK;
+    if (eng->co_target) return FP_OK;  // coalescing copies each batch into the staging batch at its submit
     const ViewArrays a = view_arrays(v);
     for (int i = 0; i < 17; i++)
         if (!a.src[i] && a.size[i]) return eng->fail(FP_BAD_INPUT, "null batch array");
@@ -402,9 +411,21 @@ fp_status fp_engine_prefetch_batch(fp_engine *eng, const fp_batch_view *v) {
 
 static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device);
 
-fp_status fp_engine_submit_batch(fp_engine *eng, const fp_batch_view *v) { return submit(eng, v, false); }
+static fp_status co_submit(fp_engine *eng, const fp_batch_view *v);
+static fp_status co_flush(fp_engine *eng);
 
-fp_status fp_engine_submit_batch_device(fp_engine *eng, const fp_batch_view *v) { return submit(eng, v, true); }
+fp_status fp_engine_submit_batch(fp_engine *eng, const fp_batch_view *v) {
+    if (eng && v && eng->co_target) return co_submit(eng, v);
+    return submit(eng, v, false);
+}
+
+fp_status fp_engine_submit_batch_device(fp_engine *eng, const fp_batch_view *v) {
+    if (eng && eng->co_target) {
+        const fp_status s = co_flush(eng);  // staged reads come first in stream order
+        if (s != FP_OK) return s;
+    }
+    return submit(eng, v, true);
+}
 
 void *fp_engine_cuda_stream(fp_engine *eng) { return eng ? reinterpret_cast<void *>(eng->st) : nullptr; }
 
@@ -550,11 +571,13 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
         w.baq_alt = reinterpret_cast<u16 *>(p); p += al(Q * 2);
         w.frac = reinterpret_cast<float *>(p);
     }
-    CK(eng->lists.ensure(al(R * 4ull) * 7 + 4096), "work lists");
+    CK(eng->lists.ensure(al(R * 4ull) * 9 + 4096), "work lists");
     w.baq_list = eng->lists.as<u32>();
     w.esc_list = w.baq_list + 3ull * R;
-    u32 *sorted_lists = w.baq_list + 5ull * R;  // classes 0 and 1 by query length
-    u32 *len_hist = w.baq_list + 7ull * R;
+    // regions of R entries: BAQ lists of band classes 0-2, escalation lists of classes 0-2, classes 0 and 1
+    // ordered by query length, then the length histogram
+    u32 *sorted_lists = w.baq_list + 6ull * R;
+    u32 *len_hist = w.baq_list + 8ull * R;
     CK(eng->entry_cnt.ensure(al((R + 1) * 4ull)), "entry counts");
     CK(eng->entry_off.ensure(al((R + 1) * 4ull)), "entry offsets");
     w.entry_count = eng->entry_cnt.as<u32>();
@@ -574,7 +597,8 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
 
     // ---- K2 BAQ ----
     const uint32_t max_q = cnt[7] ? cnt[7] : 1;  // longest BAQ query window of the batch
-    auto run_fp64 = [&](const u32 *list, const u32 *count, u32 nmax, u32 max_bw) -> fp_status {
+    auto run_fp64 = [&](const u32 *list, const u32 *count, u32 nmax, u32 max_bw, u32 min_bw = 0,
+                        bool cap = true) -> fp_status {
         if (!nmax) return FP_OK;
         const u32 threads = std::min<u32>(baq64_threads(), ((nmax + 127) / 128) * 128);
         u64 need = baq64_scratch_doubles(threads, max_q, max_bw);
@@ -582,8 +606,9 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
         if (need > budget) need = std::max<u64>(budget, baq64_scratch_doubles(128, max_q, max_bw));
         CK(eng->s64.ensure(need * 8), "FP64 BAQ scratch");
         eng->s64_doubles = eng->s64.cap / 8;
-        launch_baq64(b, eng->ref, w, list, count, nmax, eng->s64.as<double>(), eng->s64_doubles, max_q, max_bw, st);
-        launch_cap(b, w, list, count, 1, st, nmax);
+        launch_baq64(b, eng->ref, w, list, count, nmax, eng->s64.as<double>(), eng->s64_doubles, max_q, max_bw, st,
+                     min_bw);
+        if (cap) launch_cap(b, w, list, count, 1, st, nmax);
         return FP_OK;
     };
     fp_status s;
@@ -606,8 +631,8 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
             if (c == 0 && n_cls[0]) { cudaEventRecord(eng->ev[11], st); timed_main = true; }
         }
     } else {
-        // FP32 with certified bounds (band classes 0 and 1), exact FP64 replay of the undecided reads, and the
-        // thread-per-read FP64 kernel for bands wider than 15. Band class 1 (few reads, latency-bound kernels)
+        // FP32 with certified bounds (band classes 0 and 1), exact FP64 replay of the undecided reads, and exact
+        // FP64 for bands wider than 15. Band class 1 (few reads, latency-bound kernels)
         // runs on a second stream with its own scratch and work counters, alongside the class-0 kernels.
         const u64 budget = u64(3) << 30, budget1 = u64(1) << 30;
         CK(eng->s32.ensure(budget), "BAQ scratch");
@@ -623,8 +648,8 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
         auto run_replay = [&](int c, cudaStream_t cs, void *scr, u64 scr_bytes, u32 *ctr) {
             const u32 *list = w.baq_list + size_t(c) * R;
             const u32 *esc = replay_all ? list : w.esc_list + size_t(c) * R;
-            u32 *esc_count = replay_all ? w.counters + c : w.counters + (c ? 10 : 4);
-            if (eng->replay_rpw)
+            u32 *esc_count = replay_all ? w.counters + c : w.counters + (c == 0 ? 4 : (c == 1 ? 10 : 27));
+            if (eng->replay_rpw && c < 2)
                 launch_baq_tpr(b, eng->ref, w, esc, esc_count, n_cls[c], c, true, ctr, scr, scr_bytes, max_q,
                                eng->replay_rpw, cs);
             else
@@ -646,8 +671,25 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
             run_fp32(0, st, eng->s32.p, budget, w.counters + 8);
             cudaEventRecord(eng->ev[14], st);
         }
-        // bands wider than 15: thread-per-read FP64
-        if ((s = run_fp64(w.baq_list + 2ull * R, w.counters + 2, n_cls[2], bw_max[2])) != FP_OK) return s;
+        // bands wider than 15: FP32 with certified bounds, the band across a warp's lanes, for bw <= 31 (its
+        // undecided reads join the replays); exact FP64 for wider ones (each kernel skips the others' reads; the
+        // FP64 results are final, so the capping step finds them decided)
+        if (n_cls[2]) {
+            const u32 *list2 = w.baq_list + 2ull * R;
+            // (the exact kernels below and the class-2 replay reuse the buffer)
+            const u64 exact_bytes = std::max(baq_exact_block_scratch_bytes(2, max_q),
+                                             bw_max[2] > 31 ? baq_exact_block_scratch_bytes(3, max_q) : 0);
+            CK(eng->s32w.ensure(std::max(baq_wide_scratch_bytes(n_cls[2], max_q), exact_bytes)), "BAQ scratch");
+            launch_baq_wide(b, eng->ref, w, list2, w.counters + 2, n_cls[2], w.counters + 26, eng->s32w.p,
+                            eng->s32w.cap, max_q, st);
+            // bw 32..63: exact FP64 across a warp's lanes, every row; wider: the thread-per-read FP64 kernel
+            if (bw_max[2] > 31)
+                launch_baq_exact(b, eng->ref, w, list2, w.counters + 2, n_cls[2], 3, w.counters + 29, eng->s32w.p,
+                                 eng->s32w.cap, max_q, true, st);
+            if (bw_max[2] > 63 && (s = run_fp64(list2, w.counters + 2, n_cls[2], bw_max[2], 64, false)) != FP_OK)
+                return s;
+            launch_cap(b, w, list2, w.counters + 2, 0, st, n_cls[2]);
+        }
         // every certified read now has its final BQ tags; the reads left for the replay are marked deferred.
         // The first covariate count pass runs on its own stream beside the replays (with the test hook every
         // read is replayed, so the pass waits for the whole BAQ stage instead)
@@ -671,6 +713,7 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
             run_replay(0, st, eng->s32.p, budget, w.counters + 11);
             cudaEventRecord(eng->ev[15], st);
         }
+        if (n_cls[2]) run_replay(2, st, eng->s32w.p, eng->s32w.cap, w.counters + 28);
         timed_paths = split && n_cls[0];
         if (split) CK(cudaStreamWaitEvent(st, eng->join, 0), "join");
     }
@@ -681,17 +724,18 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
     if (cov1_overlapped) CK(cudaStreamWaitEvent(st, eng->cov1_done, 0), "join");
     else count_first_pass(st);
     if (eng->baq_mode != FP_BAQ_FP64) {
-        for (int c = 0; c < 2; c++)
-            launch_cov_count_list(b, w, eng->tables, w.esc_list + size_t(c) * R, w.counters + (c ? 10 : 4), n_cls[c],
-                                  st);
+        for (int c = 0; c < 3; c++)
+            launch_cov_count_list(b, w, eng->tables, w.esc_list + size_t(c) * R,
+                                  w.counters + (c == 0 ? 4 : (c == 1 ? 10 : 27)), n_cls[c], st);
     }
     launch_cycle_pairs(eng->tables, st);
     launch_exclusive_scan(w.entry_count, w.entry_offset, R, eng->scan_tmp.p, st);
     u32 tail[2];
     CK(cudaMemcpyAsync(&tail[0], w.entry_offset + R, 4, cudaMemcpyDeviceToHost, st), "D2H");
-    u32 esc1 = 0;
+    u32 esc1 = 0, esc2 = 0;
     CK(cudaMemcpyAsync(&tail[1], w.counters + 4, 4, cudaMemcpyDeviceToHost, st), "D2H");
     CK(cudaMemcpyAsync(&esc1, w.counters + 10, 4, cudaMemcpyDeviceToHost, st), "D2H");
+    CK(cudaMemcpyAsync(&esc2, w.counters + 27, 4, cudaMemcpyDeviceToHost, st), "D2H");
     CK(cudaStreamSynchronize(st), "covariates");
     const u64 N = tail[0];
     CK(eng->entries.ensure(al(N * 8 + 8)), "entries");
@@ -731,7 +775,7 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
     eng->stats.total_reads += R;
     eng->stats.filtered_reads += cnt[5];
     eng->stats.baq_reads += cnt[6];
-    eng->stats.baq_fp64_escalated_reads += u64(tail[1]) + esc1;
+    eng->stats.baq_fp64_escalated_reads += u64(tail[1]) + esc1 + esc2;
     for (int c = 0; c < 3; c++) {
         eng->stats.baq_reads_by_band[c] += n_cls[c];
         eng->stats.baq_band_cells[c] += cells[c];
@@ -739,7 +783,7 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
     eng->stats.baq_escalated_by_cause[0] += cause[0];
     eng->stats.baq_escalated_by_cause[1] += cause[1];
     eng->stats.baq_escalated_by_band[0] += tail[1];
-    eng->stats.baq_escalated_by_band[1] += esc1;
+    eng->stats.baq_escalated_by_band[1] += u64(esc1) + esc2;
     if (timed_paths) {
         const int ids[4] = {14, 15, 12, 13};
         for (int k = 0; k < 4; k++)
@@ -755,6 +799,131 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
     return FP_OK;
 }
 
+// ---- coalescing of small host batches ----
+// Array i of a batch view counts reads (dim 0), cigar ops (1), read words (2) or qualities (3).
+static const int kCoDim[17] = {0, 0, 0, 0, 0, 1, 0, 0, 2, 0, 0, 3, 0, 0, 0, 0, 0};
+static const int kCoElem[17] = {2, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 1, 4, 4, 2, 1, 4};
+
+// The checks of k_validate, on the host, so that a malformed batch is refused at its own submit.
+static fp_status validate_host(fp_engine *eng, const fp_batch_view *v, const ViewArrays &va) {
+    for (int i = 0; i < 17; i++)
+        if (!va.src[i] && va.size[i]) return eng->fail(FP_BAD_INPUT, "null batch array");
+    u32 e = 0;
+    for (uint32_t r = 0; r < v->num_reads; r++) {
+        if (uint64_t(v->cigar_start[r]) + v->cigar_len[r] > v->num_cigar_ops) e |= ERR_BAD_READ_RANGE;
+        if (uint64_t(v->read_start[r]) + v->read_len[r] > v->num_read_symbols) e |= ERR_BAD_READ_RANGE;
+        if (uint64_t(v->qual_start[r]) + v->qual_len[r] > v->num_qualities) e |= ERR_BAD_READ_RANGE;
+        if (v->read_len[r] > MAX_READ_LEN) e |= ERR_READ_TOO_LONG;
+        if (v->read_group[r] != U32_NONE && v->read_group[r] >= eng->n_rg) e |= ERR_BAD_READ_GROUP;
+    }
+    if (!e) return FP_OK;
+    std::string m = "batch rejected:";
+    if (e & ERR_BAD_READ_RANGE) m += " read/cigar/quality range outside the batch arrays;";
+    if (e & ERR_READ_TOO_LONG) m += " read longer than 511 bases (10-bit cycle covariate);";
+    if (e & ERR_BAD_READ_GROUP) m += " read group id >= num_read_groups;";
+    return eng->fail(FP_BAD_INPUT, m);
+}
+
+// Processes the staged reads as one device batch (nothing to do when none are staged).
+static fp_status co_flush(fp_engine *eng) {
+    if (eng->co_n[0] == 0) return FP_OK;
+    char *base = eng->co_buf.as<char>();
+    const void *p[17];
+    for (int i = 0; i < 17; i++) p[i] = base + eng->co_off[i];
+    fp_batch_view v;
+    v.num_reads = uint32_t(eng->co_n[0]);
+    v.num_cigar_ops = uint32_t(eng->co_n[1]);
+    v.num_read_symbols = eng->co_n[2] * 8;
+    v.num_qualities = eng->co_n[3];
+    v.chromosome = (const uint16_t *)p[0];
+    v.alignment_start = (const uint32_t *)p[1];
+    v.alignment_stop = (const uint32_t *)p[2];
+    v.mate_alignment_start = (const uint32_t *)p[3];
+    v.inferred_insert_size = (const int32_t *)p[4];
+    v.cigars = (const uint32_t *)p[5];
+    v.cigar_start = (const uint32_t *)p[6];
+    v.cigar_len = (const uint32_t *)p[7];
+    v.reads = (const uint32_t *)p[8];
+    v.read_start = (const uint32_t *)p[9];
+    v.read_len = (const uint32_t *)p[10];
+    v.qualities = (const uint8_t *)p[11];
+    v.qual_start = (const uint32_t *)p[12];
+    v.qual_len = (const uint32_t *)p[13];
+    v.flags = (const uint16_t *)p[14];
+    v.mapq = (const uint8_t *)p[15];
+    v.read_group = (const uint32_t *)p[16];
+    const uint64_t batches = eng->stats.num_batches;
+    const fp_status s = submit(eng, &v, true);
+    for (auto &x : eng->co_n) x = 0;
+    eng->stats.num_batches = batches;  // input batches are counted as they are staged
+    return s;
+}
+
+static fp_status co_submit(fp_engine *eng, const fp_batch_view *v) {
+    if (eng->finalized) return eng->fail(FP_NOT_READY, "submit after finalize; call fp_engine_reset first");
+    if (v->num_reads == 0) {
+        eng->stats.num_batches++;
+        return FP_OK;
+    }
+    CK(cudaSetDevice(eng->device), "set device");
+    const ViewArrays va = view_arrays(v);
+    fp_status s = validate_host(eng, v, va);
+    if (s != FP_OK) return s;
+    const uint64_t need[4] = {v->num_reads, v->num_cigar_ops, (v->num_read_symbols + 7) / 8, v->num_qualities};
+    if (need[0] >= eng->co_target) {  // large enough alone: the staged reads first, then this batch
+        s = co_flush(eng);
+        if (s != FP_OK) return s;
+        return submit(eng, v, false);
+    }
+    // the staged batch must stay within the 32-bit counts and offsets of a batch view
+    const uint64_t lim[4] = {0xFFFFFFFFull, 0xFFFFFFFFull, 0xFFFFFFFFull / 8, 0xFFFFFFFFull};
+    bool fits = true, room = true;
+    for (int d = 0; d < 4; d++) {
+        if (eng->co_n[d] + need[d] > lim[d]) fits = false;
+        if (eng->co_n[d] + need[d] > eng->co_cap[d]) room = false;
+    }
+    if (!fits || !room) {
+        s = co_flush(eng);
+        if (s != FP_OK) return s;
+    }
+    if (!room) {
+        // (empty now) capacity for about two targets' worth of reads at this batch's density
+        uint64_t cap[4];
+        cap[0] = std::max<uint64_t>(2ull * eng->co_target, need[0]);
+        for (int d = 1; d < 4; d++)
+            cap[d] = std::max<uint64_t>(eng->co_cap[d],
+                                        std::max<uint64_t>(need[d], (2ull * eng->co_target * need[d] + need[0] - 1) / need[0]));
+        size_t total = 0, off[17];
+        for (int i = 0; i < 17; i++) {
+            off[i] = total;
+            total += al(std::max<uint64_t>(1, cap[kCoDim[i]]) * kCoElem[i]);
+        }
+        eng->co_buf.release();
+        CK(eng->co_buf.ensure(total), "coalescing buffer");
+        for (int i = 0; i < 17; i++) eng->co_off[i] = off[i];
+        for (int d = 0; d < 4; d++) eng->co_cap[d] = cap[d];
+    }
+    cudaStream_t st = eng->st;
+    char *base = eng->co_buf.as<char>();
+    for (int i = 0; i < 17; i++) {
+        if (!va.size[i]) continue;
+        CK(cudaMemcpyAsync(base + eng->co_off[i] + eng->co_n[kCoDim[i]] * kCoElem[i], va.src[i], va.size[i],
+                           cudaMemcpyHostToDevice, st), "coalescing copy");
+    }
+    u32 *starts[3];
+    const int idx[3] = {6, 9, 12};  // cigar_start, read_start, qual_start
+    for (int k = 0; k < 3; k++)
+        starts[k] = reinterpret_cast<u32 *>(base + eng->co_off[idx[k]]) + eng->co_n[0];
+    launch_rebase_starts(starts[0], starts[1], starts[2], v->num_reads, u32(eng->co_n[1]), u32(eng->co_n[2] * 8),
+                         u32(eng->co_n[3]), st);
+    CK(cudaGetLastError(), "coalescing rebase");
+    CK(cudaStreamSynchronize(st), "coalescing copy");  // the host buffers may be reused from here on
+    for (int d = 0; d < 4; d++) eng->co_n[d] += need[d];
+    eng->stats.num_batches++;
+    if (eng->co_n[0] >= eng->co_target) return co_flush(eng);
+    return FP_OK;
+}
+
 }  // extern "C"
 
 extern "C" {
@@ -762,6 +931,10 @@ extern "C" {
 fp_status fp_engine_finalize(fp_engine *eng) {
     if (!eng) return FP_BAD_INPUT;
     CK(cudaSetDevice(eng->device), "set device");
+    if (eng->co_target && !eng->finalized) {
+        const fp_status s0 = co_flush(eng);
+        if (s0 != FP_OK) return s0;
+    }
     cudaStream_t st = eng->st;
     cudaEventRecord(eng->ev[7], st);
     const KeySpace ks = eng->tables.ks;
@@ -933,6 +1106,7 @@ fp_status fp_engine_reset(fp_engine *eng) {
     CK(cudaMemsetAsync(eng->tab_stage.p, 0, n * sizeof(u32), eng->st), "reset");
     CK(cudaMemsetAsync(eng->tab_cyc.p, 0, size_t(eng->n_rg) * 2 * CYC_DIFF_LEN * sizeof(int), eng->st), "reset");
     eng->staged_bases = 0;
+    for (auto &x : eng->co_n) x = 0;  // staged reads of the previous job are dropped
     CK(cudaStreamSynchronize(eng->st), "reset");
     for (auto &t : eng->out) t = HostTable();
     eng->finalized = false;

@@ -35,7 +35,7 @@ __device__ __forceinline__ double calc_eps(u8 ref, u8 read, u8 q) {
 }
 
 __global__ void __launch_bounds__(THREADS) k_baq64(DevBatch b, DevRef ref, BatchWork w, const u32 *list,
-                                                   const u32 *count, double *scratch, u64 per_thread) {
+                                                   const u32 *count, double *scratch, u64 per_thread, int min_bw) {
     const u32 tid = blockIdx.x * blockDim.x + threadIdx.x;
     const u32 nthreads = gridDim.x * blockDim.x;
     const u32 n = *count;
@@ -46,6 +46,7 @@ __global__ void __launch_bounds__(THREADS) k_baq64(DevBatch b, DevRef ref, Batch
 
     for (u32 li = tid; li < n; li += nthreads) {
         const u32 r = list[li];
+        if (int(w.bw[r]) < min_bw) continue;  // (narrower bands are computed by another kernel)
         const u16 *win = w.win + size_t(r) * 8;
         const int qx = win[0], qy = win[1];
         const int hx = w.hmm[size_t(r) * 2], hy = w.hmm[size_t(r) * 2 + 1];
@@ -236,7 +237,8 @@ void baq64_set_constants(const HmmConst &c) {
 }
 
 void launch_baq64(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
-                  u32 max_reads, double *scratch, u64 scratch_doubles, u32 max_qlen, u32 max_bw, cudaStream_t s) {
+                  u32 max_reads, double *scratch, u64 scratch_doubles, u32 max_qlen, u32 max_bw, cudaStream_t s,
+                  u32 min_bw) {
     if (!max_reads) return;
     const u64 row = u64(max_bw * 2 + 1) * 3 + 6;
     const u64 per = u64(max_qlen + 1) * row * 2 + (max_qlen + 2);
@@ -247,7 +249,7 @@ void launch_baq64(const DevBatch &b, const DevRef &ref, const BatchWork &w, cons
     const u64 need = (max_reads + THREADS - 1) / THREADS;
     if (need < blocks) blocks = need;
     if (blocks == 0) return;  // caller guarantees room for at least one block
-    k_baq64<<<u32(blocks), THREADS, 0, s>>>(b, ref, w, list, count, scratch, per);
+    k_baq64<<<u32(blocks), THREADS, 0, s>>>(b, ref, w, list, count, scratch, per, int(min_bw));
     g_kernel_launches++;
 }
 

@@ -41,7 +41,7 @@ __device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b
 template <int G, int NS>
 __global__ void __launch_bounds__(EX_THREADS) k_baq_exact(DevBatch b, DevRef dref, BatchWork w, const u32 *list,
                                                           const u32 *count, u32 *work_ctr, double *scratch,
-                                                          u32 max_q, int full) {
+                                                          u32 max_q, int full, int min_wc) {
     constexpr int WC = G * NS;          // band slots per read
     constexpr int GPW = 32 / G;         // reads (groups) per warp
     constexpr int WPB = EX_THREADS / 32;
@@ -77,8 +77,11 @@ __global__ void __launch_bounds__(EX_THREADS) k_baq_exact(DevBatch b, DevRef dre
         base = __shfl_sync(FULL, base, 0);
         if (base >= n_list) break;
         const u32 li = base + g;
-        const bool has = li < n_list;
+        bool has = li < n_list;
         const u32 r = has ? list[li] : 0;
+        // a read whose band does not fit the group's slots is left to a wider kernel (or the thread-per-read
+        // one), a read whose band fits min_wc slots to the narrower kernel that took it
+        if (has && (2 * int(w.bw[r]) + 1 > WC || 2 * int(w.bw[r]) + 1 <= min_wc)) has = false;
 
         // ---- setup (device/baq.cu:247-334), identical for the lanes of a group ----
         int qL = 0, refLen = 0, bmLen = 1, bw = 0;
@@ -182,6 +185,10 @@ __global__ void __launch_bounds__(EX_THREADS) k_baq_exact(DevBatch b, DevRef dre
             const int x = i - bw > 0 ? i - bw : 0;
             const bool slide = i > bw;
             const u8 qy = act ? QRY(i - 1) : 0, qq = act ? QUL(i - 1) : 0;
+            // the serial loops below visit only the slots that hold band cells of some group of the warp: every
+            // other slot holds zeros, which change neither a sum nor the D chain (bit for bit)
+            const int slo = int(__reduce_min_sync(FULL, u32(act ? (beg - x > 0 ? beg - x : 0) : WC)));
+            const int shi = int(__reduce_max_sync(FULL, u32(act ? (end - x < WC - 1 ? end - x : WC - 1) : 0)));
             // phase A: M and I of every slot from the previous row; m2 * M feeds the D chain of the next slot
             double mI[NS];
 #pragma unroll
@@ -206,9 +213,8 @@ __global__ void __launch_bounds__(EX_THREADS) k_baq_exact(DevBatch b, DevRef dre
             // phase B1: D(k) = m2 * M(k-1) + m8 * D(k-1) along the row (zero below the band; past it the chain
             // runs on but those slots are discarded)
             if (l == 0) {
-                double d = 0.0;
-#pragma unroll
-                for (int s = 0; s < WC; s++) {
+                double d = 0.0;  // (zero at and below the lowest band slot: M below the band is zero)
+                for (int s = slo; s <= shi; s++) {
                     d = da(s == 0 ? 0.0 : X0[s], dm(m8, d));
                     X1[s] = d;
                 }
@@ -227,8 +233,7 @@ __global__ void __launch_bounds__(EX_THREADS) k_baq_exact(DevBatch b, DevRef dre
             double inv = 0.0;
             if (l == 0) {
                 double sum = 0.0;
-#pragma unroll
-                for (int s = 0; s < WC; s++) sum = da(sum, X2[s]);
+                for (int s = slo; s <= shi; s++) sum = da(sum, X2[s]);
                 if (act) {
                     FROW(i)[2 * WC] = sum;
                     inv = __ddiv_rn(1.0, sum);
@@ -294,6 +299,9 @@ __global__ void __launch_bounds__(EX_THREADS) k_baq_exact(DevBatch b, DevRef dre
             const int beg = 1 > i - bw ? 1 : i - bw;
             const int end = refLen < i + bw ? refLen : i + bw;
             const int x = i - bw > 0 ? i - bw : 0;
+            const bool on = i >= 1 && i <= qL;
+            const int slo = int(__reduce_min_sync(FULL, u32(on ? (beg - x > 0 ? beg - x : 0) : WC)));
+            const int shi = int(__reduce_max_sync(FULL, u32(on ? (end - x < WC - 1 ? end - x : WC - 1) : 0)));
             if (t > 0) {
                 const bool grow = i < bw;  // row i+1 still in the growing band
                 const bool y = i > 1;
@@ -316,10 +324,10 @@ __global__ void __launch_bounds__(EX_THREADS) k_baq_exact(DevBatch b, DevRef dre
                 __syncwarp();
                 // B_D(k) = (e * m6 + m8 * B_D(k+1)) * y, descending along the row
                 if (l == 0) {
-                    double d = 0.0;
+                    double d = 0.0;  // (zero above the highest band slot)
                     X1[WC] = 0.0;
-#pragma unroll
-                    for (int s = WC - 1; s >= 0; s--) {
+                    X1[shi + 1] = 0.0;
+                    for (int s = shi; s >= slo; s--) {
                         d = y ? da(X0[s], dm(m8, d)) : 0.0;
                         X1[s] = d;
                     }
@@ -374,8 +382,7 @@ __global__ void __launch_bounds__(EX_THREADS) k_baq_exact(DevBatch b, DevRef dre
             __syncwarp();
             if (l == 0 && need) {
                 double sum = 0.0;
-#pragma unroll
-                for (int q = 0; q < 2 * WC; q++) sum = da(sum, X2[q]);
+                for (int q = 2 * slo; q <= 2 * shi + 1; q++) sum = da(sum, X2[q]);
                 FROW(i)[2 * WC + 1] = __longlong_as_double((long long)best);
                 FROW(i)[2 * WC + 2] = sum;
                 // the reference keeps max_k = -1 when no term exceeds 0
@@ -401,7 +408,8 @@ __global__ void __launch_bounds__(EX_THREADS) k_baq_exact(DevBatch b, DevRef dre
 
 template <int G, int NS>
 void launch_g(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
-              u32 max_reads, u32 *ctr, double *scratch, u64 scratch_elems, u32 max_q, int full, cudaStream_t s) {
+              u32 max_reads, u32 *ctr, double *scratch, u64 scratch_elems, u32 max_q, int full, cudaStream_t s,
+              int min_wc = 0) {
     constexpr int WC = G * NS, GPW = 32 / G;
     const u64 per_group = (u64(max_q) + 2) * (2 * WC + 3);
     const u64 groups = scratch_elems / per_group;
@@ -412,11 +420,21 @@ void launch_g(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u3
     if (blocks > 152 * 8) blocks = 152 * 8;
     if (blocks == 0) return;
     cudaMemsetAsync(ctr, 0, sizeof(u32), s);
-    k_baq_exact<G, NS><<<u32(blocks), EX_THREADS, 0, s>>>(b, ref, w, list, count, ctr, scratch, max_q, full);
+    k_baq_exact<G, NS><<<u32(blocks), EX_THREADS, 0, s>>>(b, ref, w, list, count, ctr, scratch, max_q, full, min_wc);
     g_kernel_launches++;
 }
 
 }  // namespace
+
+u64 baq_exact_block_scratch_bytes(int band_class, u32 max_q) {
+    // one block of each kernel a band class uses (GPW groups per warp, 2 warps): the launches size their grids
+    // by the groups the scratch holds and launch nothing below one block
+    auto block = [&](int wc, int gpw) { return u64(gpw) * (EX_THREADS / 32) * (u64(max_q) + 2) * (2 * wc + 3) * 8; };
+    if (band_class == 0) return block(16, 4);
+    if (band_class == 1) return block(32, 2);
+    if (band_class == 2) return std::max(block(48, 2), block(64, 1));
+    return block(128, 1);
+}
 
 void baq_exact_set_constants(const HmmConst &c) {
     cudaMemcpyToSymbol(cx_qual2prob, c.qual2prob, sizeof(c.qual2prob));
@@ -427,14 +445,24 @@ void launch_baq_exact(const DevBatch &b, const DevRef &ref, const BatchWork &w, 
                       u32 max_reads, int band_class, u32 *ctr, void *scratch, u64 scratch_bytes, u32 max_q,
                       bool all_rows, cudaStream_t s) {
     if (!max_reads) return;
+    // band_class 3: the reads of the class-2 list with bw 32..63 (every row; the FP32 kernel skips them)
     // band class 0 (bw <= 7, 15 slots): 8 lanes x 2 slots, 4 reads per warp; class 1 (bw <= 15, 31 slots):
-    // 16 lanes x 2 slots, 2 reads per warp
-    if (band_class == 0)
-        launch_g<8, 2>(b, ref, w, list, count, max_reads, ctr, (double *)scratch, scratch_bytes / 8, max_q,
-                       all_rows ? 1 : 0, s);
-    else
-        launch_g<16, 2>(b, ref, w, list, count, max_reads, ctr, (double *)scratch, scratch_bytes / 8, max_q,
-                        all_rows ? 1 : 0, s);
+    // 16 lanes x 2 slots, 2 reads per warp; wider bands: 16 lanes x 3 slots (bw <= 23, 2 reads per warp), then
+    // 32 lanes x 2 slots for the rest up to bw 31 (a read per warp; the second launch reuses the work counter
+    // after the first finishes on the same stream)
+    double *d = (double *)scratch;
+    const int full = all_rows ? 1 : 0;
+    if (band_class == 0) {
+        launch_g<8, 2>(b, ref, w, list, count, max_reads, ctr, d, scratch_bytes / 8, max_q, full, s);
+    } else if (band_class == 1) {
+        launch_g<16, 2>(b, ref, w, list, count, max_reads, ctr, d, scratch_bytes / 8, max_q, full, s);
+    } else if (band_class == 2) {
+        launch_g<16, 3>(b, ref, w, list, count, max_reads, ctr, d, scratch_bytes / 8, max_q, full, s);
+        launch_g<32, 2>(b, ref, w, list, count, max_reads, ctr, d, scratch_bytes / 8, max_q, full, s, 48);
+    } else {
+        // bands of 64..127 slots (bw 32..63): 32 lanes x 4 slots
+        launch_g<32, 4>(b, ref, w, list, count, max_reads, ctr, d, scratch_bytes / 8, max_q, full, s, 64);
+    }
 }
 
 }  // namespace fpg

@@ -32,6 +32,15 @@ __global__ void k_validate(DevBatch b, u32 n_rg, u32 *err) {
     if (e) raise_error(err, e);
 }
 
+__global__ void k_rebase_starts(u32 *cigar_start, u32 *read_start, u32 *qual_start, u32 n, u32 d_cigar, u32 d_sym,
+                                u32 d_qual) {
+    const u32 r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    cigar_start[r] += d_cigar;
+    read_start[r] += d_sym;
+    qual_start[r] += d_qual;
+}
+
 __global__ void k_op_lengths(DevBatch b, u32 *out) {
     const u32 i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < b.num_cigar_ops) out[i] = op_len(b.cigars[i]);
@@ -707,9 +716,9 @@ __global__ void __launch_bounds__(64) k_cap(DevBatch b, BatchWork w, const u32 *
         const bool need_update = readI_total == u32(wcl.y - wcl.x + 1);
         if (need_update && !exact && __any_sync(FULL, escalate)) {
             if (lane == 0) {
-                // escalation lists by band class: class 0 (band <= 7) and class 1 (band <= 15)
-                const u32 cls = w.bw[r] <= 7 ? 0 : 1;
-                const u32 slot = atomicAdd(&w.counters[cls ? 10 : 4], 1u);
+                // escalation lists by band class: class 0 (band <= 7), class 1 (band <= 15), class 2 (wider)
+                const u32 cls = w.bw[r] <= 7 ? 0 : (w.bw[r] <= 15 ? 1 : 2);
+                const u32 slot = atomicAdd(&w.counters[cls == 0 ? 4 : (cls == 1 ? 10 : 27)], 1u);
                 w.esc_list[size_t(cls) * b.R + slot] = r;
                 w.status[r] = RS_DEFERRED;
             }
@@ -765,6 +774,13 @@ __global__ void __launch_bounds__(64) k_cap(DevBatch b, BatchWork w, const u32 *
 void launch_validate(const DevBatch &b, u32 n_rg, u32 *err, cudaStream_t s) {
     if (!b.R) return;
     k_validate<<<(b.R + 255) / 256, 256, 0, s>>>(b, n_rg, err);
+    g_kernel_launches++;
+}
+
+void launch_rebase_starts(u32 *cigar_start, u32 *read_start, u32 *qual_start, u32 n, u32 d_cigar, u32 d_sym,
+                          u32 d_qual, cudaStream_t s) {
+    if (!n) return;
+    k_rebase_starts<<<(n + 255) / 256, 256, 0, s>>>(cigar_start, read_start, qual_start, n, d_cigar, d_sym, d_qual);
     g_kernel_launches++;
 }
 

@@ -71,6 +71,9 @@ struct HmmConst {
 // k_prep.cu
 void launch_validate(const DevBatch &b, u32 n_rg, u32 *err, cudaStream_t s);
 void launch_op_lengths(const DevBatch &b, u32 *out, cudaStream_t s);
+// batch coalescing: adds the staged totals to the start offsets of n appended reads
+void launch_rebase_starts(u32 *cigar_start, u32 *read_start, u32 *qual_start, u32 n, u32 d_cigar, u32 d_sym,
+                          u32 d_qual, cudaStream_t s);
 void launch_prep(const DevBatch &b, const DevRef &ref, const BatchWork &w, cudaStream_t s);
 // BAQ lists of band classes 0 and 1 ordered by query length into sorted (2 x R entries); hist: 1024 words
 void launch_sort_baq_lists(const BatchWork &w, u32 R, u32 max_class_reads, u32 *hist, u32 *sorted, cudaStream_t s);
@@ -80,7 +83,8 @@ void launch_cap(const DevBatch &b, const BatchWork &w, const u32 *list, const u3
 // k_baq64.cu
 void baq64_set_constants(const HmmConst &c);
 void launch_baq64(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
-                  u32 max_reads, double *scratch, u64 scratch_doubles, u32 max_qlen, u32 max_bw, cudaStream_t s);
+                  u32 max_reads, double *scratch, u64 scratch_doubles, u32 max_qlen, u32 max_bw, cudaStream_t s,
+                  u32 min_bw = 0);  // reads of the list with a band narrower than min_bw are skipped
 u64 baq64_scratch_doubles(u32 threads, u32 max_qlen, u32 max_bw);
 u32 baq64_threads();
 
@@ -88,6 +92,12 @@ u32 baq64_threads();
 void baq_tpr_set_constants(const HmmConst &c);
 // k_baq_exact.cu (exact FP64 replay, a group of lanes per read)
 void baq_exact_set_constants(const HmmConst &c);
+u64 baq_exact_block_scratch_bytes(int band_class, u32 max_q);  // scratch of one block of the class's kernels
+// FP32 certified BAQ for bands wider than 15 (bw <= 31; wider ones are skipped), the band across a warp's lanes
+void baq_wide_set_constants(const HmmConst &c);
+u64 baq_wide_scratch_bytes(u32 reads, u32 max_q);
+void launch_baq_wide(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
+                     u32 max_reads, u32 *ctr, void *scratch, u64 scratch_bytes, u32 max_q, cudaStream_t s);
 void launch_baq_exact(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
                       u32 max_reads, int band_class, u32 *ctr, void *scratch, u64 scratch_bytes, u32 max_q,
                       bool all_rows, cudaStream_t s);

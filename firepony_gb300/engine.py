@@ -109,11 +109,12 @@ class Engine:
     """One GB300 BQSR engine (fp_engine handle)."""
 
     def __init__(self, num_read_groups: int = 1, baq_mode: str = "fp32", device: int = 0,
-                 replay_reads_per_warp: int = 0, flags: int = 0):
+                 replay_reads_per_warp: int = 0, flags: int = 0, coalesce_reads: int = 0):
         o = FpOptions()
         o.device = device
         o.replay_reads_per_warp = replay_reads_per_warp
         o.flags = flags
+        o.coalesce_reads = coalesce_reads
         o.baq_mode = FP_BAQ_FP64 if baq_mode == "fp64" else FP_BAQ_FP32
         o.num_read_groups = num_read_groups
         h = C.c_void_p()

@@ -252,6 +252,11 @@ class Batch:
         return Batch(out, len(read_ids), ncig, nsym, nq)
 
 
+def uneven_batch_sizes(num_batches: int, lo: int = 2000, hi: int = 40000, seed: int = 2) -> np.ndarray:
+    """Batch sizes drawn uniformly from [lo, hi] (the uneven-batch workload: many input batches of 2k-40k reads)."""
+    return np.random.default_rng(seed).integers(lo, hi + 1, size=num_batches)
+
+
 def unpack4(words: np.ndarray, n: int) -> np.ndarray:
     w = np.asarray(words, dtype=np.uint32)
     sh = (np.arange(8, dtype=np.uint32) * 4)

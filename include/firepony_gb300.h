@@ -63,6 +63,13 @@ typedef struct {
                                         (0 = default). Fewer reads per warp spread a small replay set over
                                         more of the GPU's FP64 units */
     uint32_t flags;              /* FP_FLAG_* bits (0 for normal operation) */
+    uint32_t coalesce_reads;     /* 0: every fp_engine_submit_batch is processed as its own device batch.
+                                    N > 0: host batches smaller than N reads are validated on the host, copied
+                                    into a device staging batch (offsets rebased) and processed together once
+                                    N reads are staged; finalize and fp_engine_submit_batch_device process the
+                                    staged reads first. Stream order is kept, so the tables are the same.
+                                    No reference counterpart (the reference runs each io_thread batch alone). */
+    uint32_t reserved;
 } fp_options;
 
 /* Test hook: in FP32 mode, run every BAQ read of band width <= 15 through the exact FP64 replay as well
@@ -123,7 +130,8 @@ typedef struct {
     uint64_t gpu_kernel_launches;        /* kernels launched by this engine since creation */
     double   gpu_ms_per_stage[8];        /* device time per stage (see fp_stage) */
     uint64_t baq_reads_by_band[3];       /* BAQ reads by band class: bw <= 7, bw <= 15, wider */
-    uint64_t baq_escalated_by_band[2];   /* FP32 mode: FP64 replays of band classes 0 and 1 */
+    uint64_t baq_escalated_by_band[2];   /* FP32 mode: FP64 replays of band class 0 (bw <= 7) and of the
+                                            wider classes (bw 8..15 and 16..31) */
     uint64_t baq_escalated_by_cause[2];  /* FP32 mode: replays with an undecided MAP state, with undecided
                                             qualities only */
     uint64_t baq_band_cells[3];          /* HMM band cells (row x in-band reference positions) per class */
@@ -157,7 +165,10 @@ fp_status fp_engine_set_known_sites(fp_engine *engine, uint32_t contig_id, const
 
 /* Runs the per-batch hot path on one batch and folds it into the resident covariate tables.
  * Replaces batch->download + firepony_process_batch (device/pipeline_interface.cu:206-220,
- * device/pipeline.cu:56-147). Returns once the host buffers may be reused. */
+ * device/pipeline.cu:56-147). Returns once the host buffers may be reused. With coalesce_reads set, a small
+ * batch is checked and staged here (FP_BAD_INPUT for a malformed batch, nothing staged), and the staged
+ * reads are processed by the submit that brings them to coalesce_reads (a device error then concerns all of
+ * them). */
 fp_status fp_engine_submit_batch(fp_engine *engine, const fp_batch_view *batch);
 
 /* Queues the host-to-device copy of a batch on the engine's copy stream and returns at once (no reference

@@ -104,6 +104,8 @@ def test_tables_match_oracle(native, preset, n, batch, refbp, mode):
     assert se["total_reads"] == so["total_reads"]
     assert se["filtered_reads"] == so["filtered_reads"]
     assert se["baq_reads"] == so["baq_reads"]
+    if preset == "batched_uneven":
+        assert se["baq_reads_by_band"][2] > 0  # bands wider than 15 (the exact FP64 kernel across a warp's lanes)
     assert_stages_equal(batches[-1], ge, go)
     assert_tables_equal(te, to)
 
