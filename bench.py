@@ -31,7 +31,7 @@ sys.path.insert(0, str(ROOT))
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_baq_tpr<float,15> launch on a 1M-read batch of the
 # workload, from an ncu capture of this bench (profiles/k_baq_tpr_f15_precision_1M.md)
-TRAFFIC_BYTES_PER_LAUNCH = 34.52e9
+TRAFFIC_BYTES_PER_LAUNCH = 34.93e9
 METRIC = "reads/s on 1 GB300, batched vs plain, bit-exact recal table; p50/p99 job latency"
 WORKLOAD = ("precision_20M_151bp_pe: paired-end 151 bp reads, 8 read groups (quality offsets -3..+3), "
             "5 contigs / 50 Mbp, 50k known SNPs + 5k known indels, 2% indel reads, 1% substitutions rising to 3'")
