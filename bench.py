@@ -56,8 +56,11 @@ def parse():
     ap.add_argument("--coalesce-reads", type=int, default=1_000_000, help="fp_options.coalesce_reads of its coalesced run")
     ap.add_argument("--serve-jobs", type=int, default=128, help="jobs of the serving measurement (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="job arrivals per second (Poisson)")
-    ap.add_argument("--serve-slots", type=int, default=2, help="engines of the job server")
+    ap.add_argument("--serve-slots", type=int, default=3, help="engines of the job server")
     ap.add_argument("--serve-max-reads", type=int, default=5_000_000, help="largest job (log-uniform from 1000)")
+    ap.add_argument("--serve-hbm-gb", type=float, default=10.0,
+                    help="job server admission budget: estimated device memory of the jobs running together "
+                         "(0: slots only)")
     return ap.parse_args()
 
 
@@ -200,10 +203,13 @@ def run_serving(args):
     del host
     pool = [pb.batch for pb in pinned]
     arrivals, sizes = poisson_schedule(args.serve_jobs, args.serve_rate, 1000, args.serve_max_reads, seed=3)
-    server = JobServer(ref, p.num_read_groups, slots=args.serve_slots)
+    budget = int(args.serve_hbm_gb * 1e9) if args.serve_hbm_gb > 0 else None
+    server = JobServer(ref, p.num_read_groups, slots=args.serve_slots, hbm_budget_bytes=budget)
     try:
         run_schedule(server, jobs_from_pool(pool, [20_000] * (2 * args.serve_slots), per), [0.0] * (2 * args.serve_slots))
+        server.peak_running = 0
         res = run_schedule(server, jobs_from_pool(pool, sizes, per), arrivals)
+        peak = server.peak_running
     finally:
         server.close()
         for pb in pinned:
@@ -213,7 +219,8 @@ def run_serving(args):
     reads = int(sum(r.num_reads for r in res))
     return {"workload": "serving_mixed: 3 contigs / 250 Mbp, 450k SNP + 50k indel sites, 101/151 bp reads, 8 read groups",
             "jobs": len(res), "arrivals": f"Poisson {args.serve_rate:g}/s", "sizes": f"log-uniform 1000-{args.serve_max_reads} reads",
-            "slots": args.serve_slots, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "slots": args.serve_slots, "hbm_budget_gb": args.serve_hbm_gb or None, "peak_concurrent_jobs": peak,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "mean_ms": float(lat.mean()), "max_ms": float(lat.max()), "reads": reads, "reads_per_s": reads / span,
             "errors": sum(1 for r in res if r.error)}
 

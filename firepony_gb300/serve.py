@@ -12,12 +12,17 @@ its arrival (submission) to its finished tables.
 
 The ctypes calls release the GIL, so worker threads overlap host work (batch packing, result copies) with
 the device work of other jobs.
+
+Admission by HBM footprint: with `hbm_budget_bytes` set, a job starts (in arrival order) only when a slot is
+free and the estimated device memory of the running jobs plus its own fits the budget; a job larger than
+the whole budget runs alone. A job's estimate is `Job.footprint` when given, else `estimate_job_bytes` of its
+largest batch.
 """
 from __future__ import annotations
 
-import queue
 import threading
 import time
+from collections import deque
 from dataclasses import dataclass, field
 from typing import Callable, Iterable
 
@@ -26,14 +31,27 @@ import numpy as np
 from .engine import Engine
 
 
+def estimate_job_bytes(max_batch_reads: int, mean_read_len: float = 151.0) -> int:
+    """Device memory a job's batches take in an engine beyond its resident reference, tables and fixed BAQ
+    scratch: the input arrays, expanded CIGAR events, per-read and per-base work arrays and covariate
+    entries of its largest batch (about 4.5 GB per 1M reads of 151 bp)."""
+    return int(max_batch_reads * (600 + 26 * mean_read_len))
+
+
 @dataclass
 class Job:
     """One recalibration job: its batches (host `synth.Batch`-like objects with `.view()`), produced lazily
-    by `batches()` so that packing happens on the worker thread, as an io thread would do it."""
+    by `batches()` so that packing happens on the worker thread, as an io thread would do it. `footprint`:
+    its estimated device memory in bytes (0: estimated from num_reads and max_batch_reads)."""
     job_id: int
     num_reads: int
     batches: Callable[[], Iterable]
     arrival: float = 0.0
+    footprint: int = 0
+    max_batch_reads: int = 1_000_000
+
+    def device_bytes(self) -> int:
+        return self.footprint or estimate_job_bytes(min(self.num_reads, self.max_batch_reads))
 
 
 @dataclass
@@ -60,14 +78,24 @@ class _Pending:
 
 class JobServer:
     def __init__(self, reference, num_read_groups: int, slots: int = 2, baq_mode: str = "fp32", device: int = 0,
-                 keep_tables: bool = False):
+                 keep_tables: bool = False, hbm_budget_bytes: int | None = None, engine_factory=None):
         self.keep_tables = keep_tables
+        self.hbm_budget = hbm_budget_bytes
         self.engines = []
         for _ in range(slots):
-            e = Engine(num_read_groups=num_read_groups, baq_mode=baq_mode, device=device)
-            e.load_reference(reference)
+            if engine_factory is not None:
+                e = engine_factory()
+            else:
+                e = Engine(num_read_groups=num_read_groups, baq_mode=baq_mode, device=device)
+                e.load_reference(reference)
             self.engines.append(e)
-        self._q: queue.Queue = queue.Queue()
+        self._cv = threading.Condition()
+        self._queue: deque = deque()
+        self._closing = False
+        self.in_use = 0           # estimated device bytes of the running jobs
+        self.peak_in_use = 0
+        self.running = 0
+        self.peak_running = 0
         self._threads = [threading.Thread(target=self._worker, args=(e,), daemon=True) for e in self.engines]
         for t in self._threads:
             t.start()
@@ -75,12 +103,41 @@ class JobServer:
     def submit(self, job: Job) -> _Pending:
         job.arrival = time.perf_counter()
         p = _Pending(job)
-        self._q.put(p)
+        with self._cv:
+            self._queue.append(p)
+            self._cv.notify_all()
         return p
+
+    def _admissible(self, p: _Pending) -> bool:
+        if self.hbm_budget is None or self.running == 0:
+            return True
+        return self.in_use + p.job.device_bytes() <= self.hbm_budget
+
+    def _next(self):
+        """The first queued job once it fits (arrival order: a later job never passes it), or None to stop."""
+        with self._cv:
+            while True:
+                if self._closing and not self._queue:
+                    return None
+                if self._queue and self._admissible(self._queue[0]):
+                    p = self._queue.popleft()
+                    self.in_use += p.job.device_bytes()
+                    self.running += 1
+                    self.peak_in_use = max(self.peak_in_use, self.in_use)
+                    self.peak_running = max(self.peak_running, self.running)
+                    self._cv.notify_all()
+                    return p
+                self._cv.wait()
+
+    def _release(self, p: _Pending):
+        with self._cv:
+            self.in_use -= p.job.device_bytes()
+            self.running -= 1
+            self._cv.notify_all()
 
     def _worker(self, eng: Engine):
         while True:
-            p = self._q.get()
+            p = self._next()
             if p is None:
                 return
             job = p.job
@@ -95,11 +152,13 @@ class JobServer:
             except Exception as ex:  # the job fails, the server keeps running
                 p.result = JobResult(job.job_id, job.num_reads, job.arrival, start, time.perf_counter(),
                                      error=str(ex))
+            self._release(p)
             p.event.set()
 
     def close(self):
-        for _ in self._threads:
-            self._q.put(None)
+        with self._cv:
+            self._closing = True
+            self._cv.notify_all()
         for t in self._threads:
             t.join()
         for e in self.engines:
@@ -136,7 +195,7 @@ def jobs_from_pool(pool: list, sizes, batch_reads: int) -> list[Job]:
                 if left <= 0:
                     return
 
-        jobs.append(Job(j, size, make))
+        jobs.append(Job(j, size, make, max_batch_reads=batch_reads))
     return jobs
 
 

@@ -126,3 +126,43 @@ def test_threaded_submit_error_does_not_hang():
 
     with pytest.raises(RuntimeError, match="submit failed"):
         FailingEngine().submit_threaded(endless(), buffers=3)
+
+
+def test_admission_by_hbm_footprint():
+    """Jobs start in arrival order once a slot is free and the running jobs' estimated device memory plus their
+    own fits the budget; a job larger than the budget runs alone."""
+    import time
+    from firepony_gb300.serve import Job, JobServer, run_schedule
+
+    class FakeEngine:  # host-only stand-in: a job takes one short sleep per batch
+        def reset(self):
+            pass
+
+        def submit_pipelined(self, batches):
+            for _ in batches:
+                time.sleep(0.01)
+
+        def finalize(self):
+            return {}
+
+        def close(self):
+            pass
+
+    footprints = [60, 50, 30, 10, 80, 150, 5, 45, 55, 20]
+    jobs = [Job(i, 100, (lambda: iter(range(4))), footprint=f) for i, f in enumerate(footprints)]
+    server = JobServer(None, 1, slots=3, hbm_budget_bytes=100, engine_factory=FakeEngine)
+    try:
+        results = run_schedule(server, jobs, [0.0] * len(jobs))
+    finally:
+        server.close()
+    assert all(r.error is None for r in results)
+    # arrival order of the starts (no job passes an earlier one)
+    starts = [r.start for r in results]
+    assert starts == sorted(starts)
+    # at every start, the jobs running together fit the budget (or one job runs alone)
+    for r in results:
+        live = [f for q, f in zip(results, footprints) if q.start <= r.start < q.done]
+        assert len(live) <= 3
+        assert len(live) == 1 or sum(live) <= 100, (r.job_id, live)
+    assert server.peak_running >= 2  # the budget still lets jobs run side by side
+    assert server.in_use == 0 and server.running == 0
