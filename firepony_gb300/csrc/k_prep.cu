@@ -196,25 +196,34 @@ __device__ void remove_soft_clips(const Read &rd, us2 &w) {
     }
 }
 
-// lower_bound / upper_bound (device/primitives/algorithms.h:39-100)
-__device__ u32 ref_lower_bound(u32 x, const u32 *a, u32 n) {
-    if (n == 0) return 0;
-    if (x < a[0]) return 0;
-    if (a[n - 1] < x) return n;
-    u32 base = 0, count = n;
-    while (count > 0) {
-        const u32 c2 = count / 2, mid = base + c2;
-        if (a[mid] < x) { base = mid + 1; count -= c2 + 1; } else { count = c2; }
+// lower_bound / upper_bound (device/primitives/algorithms.h:39-100) over a non-decreasing array, as a
+// 32-ary search by the whole warp: each round the lanes probe 32 evenly spaced positions and a ballot keeps
+// the stretch between the last probe below the bound and the first at or past it (3 rounds for 11k sites
+// instead of 14 dependent loads). The first index meeting the predicate is unique, so the result equals the
+// reference's binary search. Every lane gets the result; all 32 lanes must call it.
+template <typename Past>
+__device__ __forceinline__ u32 warp_first_past(const u32 *a, u32 n, int lane, Past past) {
+    u32 lo = 0, hi = n;  // the answer lies in [lo, hi]
+    while (hi - lo >= 32) {
+        const u32 step = (hi - lo + 30) / 31;  // lane 31 probes at or past hi
+        const u32 p = lo + u32(lane) * step;
+        const bool t = p < hi ? past(a[p]) : true;
+        const u32 f = u32(__ffs(__ballot_sync(0xffffffffu, t)) - 1);
+        const u32 nhi = lo + f * step;
+        if (f > 0) lo = lo + (f - 1) * step + 1;
+        hi = nhi < hi ? nhi : hi;
     }
-    return base;
+    const u32 p = lo + u32(lane);
+    const bool t = p < hi ? past(a[p]) : true;  // lane hi - lo (<= 31) always votes true
+    return lo + u32(__ffs(__ballot_sync(0xffffffffu, t)) - 1);
 }
-__device__ u32 ref_upper_bound(u32 x, const u32 *a, u32 n) {
-    u32 base = 0, count = n;
-    while (count > 0) {
-        const u32 step = count / 2, it = base + step;
-        if (!(x < a[it])) { base = it + 1; count -= step + 1; } else { count = step; }
-    }
-    return base;
+// first index with a[i] >= x
+__device__ __forceinline__ u32 warp_lower_bound(u32 x, const u32 *a, u32 n, int lane) {
+    return warp_first_past(a, n, lane, [x](u32 v) { return !(v < x); });
+}
+// first index with a[i] > x
+__device__ __forceinline__ u32 warp_upper_bound(u32 x, const u32 *a, u32 n, int lane) {
+    return warp_first_past(a, n, lane, [x](u32 v) { return x < v; });
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -424,9 +433,9 @@ __device__ void filter_known_sites_w(const Read &rd, us2 w, us2 rw, u8 *sbf, int
     if (ch >= rd.ref.num_site_contigs) return;
     const DevSites db = rd.ref.sites[ch];
     const u32 wx = rd.astart + u32(rw.x), wy = rd.astart + u32(rw.y);
-    const u32 vx = ref_lower_bound(wx, db.maxend, db.n);
+    const u32 vx = warp_lower_bound(wx, db.maxend, db.n, lane);
     if (vx >= db.n) return;
-    u32 vy = ref_upper_bound(wy, db.start, db.n);
+    u32 vy = warp_upper_bound(wy, db.start, db.n, lane);
     if (vy <= vx) return;
     if (vy >= db.n) vy = db.n - 1;
     const u32 n = rd.n;
