@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--plain-steps", type=int, default=2, help="batches through the plain FP64 path (0: skip)")
     ap.add_argument("--engine-flags", type=int, default=0, help="fp_options.flags (FP_FLAG_*) for the timed engine")
     ap.add_argument("--bam-batches", type=int, default=4, help="workload batches for the BAM input measurement (0: skip)")
+    ap.add_argument("--config-legs", action="store_true",
+                    help="also measure the plain 100k-read configuration and the large single run")
+    ap.add_argument("--large-batches", type=int, default=5, help="2M-read batches of the large single run")
     ap.add_argument("--batched-batches", type=int, default=96,
                     help="input batches of the uneven-batch measurement (0: skip)")
     ap.add_argument("--coalesce-reads", type=int, default=1_000_000, help="fp_options.coalesce_reads of its coalesced run")
@@ -177,11 +180,53 @@ def run_batched(args):
         eng.close()
     same = all(np.array_equal(tables["per_batch"][t][k], tables["coalesced"][t][k])
                for t in tables["per_batch"] for k in tables["per_batch"][t])
+    if not args.no_cpu_baseline:
+        out["cpu_oracle"] = cpu_baseline(ref, batches, args.cpu_sample_seconds / 3)
     return {"workload": "batched_uneven: 4 contigs / 100 Mbp, reads of 36/76/101/151/250 bp, 0-8 indels per read, "
                         "10% wide deletions, 16 read groups",
             "batches": len(sizes), "reads": reads, "batch_reads": "uniform 2000-40000", "coalesce_reads": args.coalesce_reads,
             **out, "speedup": out["coalesced_reads_per_s"] / out["per_batch_reads_per_s"], "tables_identical": bool(same),
             "inputs": "page-locked host buffers through fp_engine_submit_batch (copies in the timed region)"}
+
+
+def run_config_legs(args):
+    """The plain configuration (1 Mbp contig, 100k single-end 101 bp reads, one read group) and the large single
+    run (3 contigs / 250 Mbp, 151 bp pairs, 32 read groups, 5% duplicates and 1% unmapped reads filtered, 3.3M
+    known sites) through the C ABI from page-locked host buffers, FP32 and plain FP64, with the CPU oracle on a
+    bounded sample of each. The large run streams `--large-batches` 2M-read batches of its 100M-read workload
+    into one resident set of tables (the reads processed are stated)."""
+    import numpy as np
+    from firepony_gb300 import synth
+    from firepony_gb300.engine import Engine, PinnedBatch
+    out = {}
+    for name, preset, nb, per in (("plain_100k_101bp", "plain_100k_101bp", 1, 100_000),
+                                  ("large_100M_151bp_pe", "large_100M_151bp_pe", args.large_batches, 2_000_000)):
+        p = synth.PRESETS[preset]
+        ref = synth.Reference(p)
+        with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+            batches = list(ex.map(lambda i: ref.batch(i, per), range(nb)))
+        pinned = [PinnedBatch(b) for b in batches]
+        reads = nb * per
+        row = {"reads": reads}
+        tables = {}
+        for mode in ("fp32", "fp64"):
+            eng = Engine(num_read_groups=p.num_read_groups, baq_mode=mode)
+            eng.load_reference(ref)
+            eng.submit_pipelined([pinned[0].batch])  # warm-up
+            eng.finalize()
+            eng.reset()
+            t0 = time.perf_counter()
+            eng.submit_pipelined([pb.batch for pb in pinned])
+            tables[mode] = eng.finalize()
+            row[mode + "_reads_per_s"] = reads / (time.perf_counter() - t0)
+            eng.close()
+        row["fp32_fp64_tables_identical"] = all(np.array_equal(tables["fp32"][t][k], tables["fp64"][t][k])
+                                                for t in tables["fp32"] for k in tables["fp32"][t])
+        row["cpu_oracle"] = cpu_baseline(ref, batches, args.cpu_sample_seconds / 3)
+        for pb in pinned:
+            pb.close()
+        out[name] = row
+    return out
 
 
 def run_serving(args):
@@ -493,6 +538,7 @@ def main():
         serving = run_serving(args) if args.serve_jobs > 0 and world == 1 else None
         bam_in = run_bam(args, res) if args.bam_batches > 0 and world == 1 else None
         batched = run_batched(args) if args.batched_batches > 0 and world == 1 else None
+        configs = run_config_legs(args) if args.config_legs and world == 1 else None
         line = {"metric": METRIC, "value": value, "unit": "reads/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
@@ -508,6 +554,7 @@ def main():
                 "serving": serving,
                 "bam": bam_in,
                 "batched": batched,
+                "configs": configs,
                 "clocks": res["clocks"],
                 "stage_ms": [round(x, 3) for x in res["stage_ms"]],
                 "baq_reads": res["stats"]["baq_reads"],
