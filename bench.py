@@ -30,7 +30,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_baq_tpr<float,15> launch on a 1M-read batch of the
-# workload, from an ncu capture of this bench (profiles/k_baq_tpr_f15_precision_1M.md)
+# workload, from an ncu capture of this bench (`--set full -k regex:k_baq_tpr -s 1 -c 1` on one 1M-read batch)
 TRAFFIC_BYTES_PER_LAUNCH = 34.93e9
 METRIC = "reads/s on 1 GB300, batched vs plain, bit-exact recal table; p50/p99 job latency"
 WORKLOAD = ("precision_20M_151bp_pe: paired-end 151 bp reads, 8 read groups (quality offsets -3..+3), "
@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--replay-rpw", type=int, default=0, help="reads per warp of the FP64 replay kernels (0: default)")
     ap.add_argument("--plain-steps", type=int, default=2, help="batches through the plain FP64 path (0: skip)")
     ap.add_argument("--engine-flags", type=int, default=0, help="fp_options.flags (FP_FLAG_*) for the timed engine")
-    ap.add_argument("--bam-batches", type=int, default=4, help="workload batches for the BAM input measurement (0: skip)")
+    ap.add_argument("--bam-batches", type=int, default=8, help="workload batches for the BAM input measurement (0: skip)")
     ap.add_argument("--config-legs", action="store_true",
                     help="also measure the plain 100k-read configuration and the large single run")
     ap.add_argument("--large-batches", type=int, default=5, help="2M-read batches of the large single run")
