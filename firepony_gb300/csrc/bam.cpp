@@ -149,14 +149,14 @@ int inflate_blocks(fpb_reader *r, int max_blocks) {
     return int(blks.size());
 }
 
-// ensures n undecoded bytes are available, inflating up to max_blocks blocks at a time; false if the stream
-// ends first
-bool need(fpb_reader *r, size_t n, int max_blocks = 512) {
+// ensures n undecoded bytes are available, inflating up to max_blocks blocks at a time: 1 when they are, 0 if
+// the stream ends first, -1 on a malformed block (r->err set)
+int need(fpb_reader *r, size_t n, int max_blocks = 512) {
     while (r->ubuf.size() - r->upos < n) {
         const int k = inflate_blocks(r, max_blocks);
-        if (k <= 0) return false;
+        if (k <= 0) return k < 0 ? -1 : 0;
     }
-    return true;
+    return 1;
 }
 
 }  // namespace
@@ -232,19 +232,19 @@ int fpb_open(const char *path, int threads, fpb_reader **out) {
     if (!r->f) { delete r; return -1; }
     // magic, text, targets: inflated a block at a time, so that the records after the header stay compressed
     // for whichever decoder (host or GPU) reads them
-    if (!need(r, 12, 1) || memcmp(r->ubuf.data() + r->upos, "BAM\1", 4) != 0) { fpb_close(r); return -1; }
+    if (need(r, 12, 1) <= 0 || memcmp(r->ubuf.data() + r->upos, "BAM\1", 4) != 0) { fpb_close(r); return -1; }
     const uint32_t l_text = rd32(r->ubuf.data() + r->upos + 4);
-    if (!need(r, 12 + size_t(l_text), 1)) { fpb_close(r); return -1; }
+    if (need(r, 12 + size_t(l_text), 1) <= 0) { fpb_close(r); return -1; }
     const std::string text(reinterpret_cast<const char *>(r->ubuf.data() + r->upos + 8), l_text);
     r->upos += 8 + l_text;
     parse_read_groups(r, text);
-    if (!need(r, 4, 1)) { fpb_close(r); return -1; }
+    if (need(r, 4, 1) <= 0) { fpb_close(r); return -1; }
     const uint32_t n_ref = rd32(r->ubuf.data() + r->upos);
     r->upos += 4;
     for (uint32_t i = 0; i < n_ref; i++) {
-        if (!need(r, 4, 1)) { fpb_close(r); return -1; }
+        if (need(r, 4, 1) <= 0) { fpb_close(r); return -1; }
         const uint32_t l_name = rd32(r->ubuf.data() + r->upos);
-        if (!need(r, 8 + size_t(l_name), 1)) { fpb_close(r); return -1; }
+        if (need(r, 8 + size_t(l_name), 1) <= 0) { fpb_close(r); return -1; }
         const char *nm = reinterpret_cast<const char *>(r->ubuf.data() + r->upos + 4);
         r->target_names.emplace_back(nm, strnlen(nm, l_name));
         r->target_lens.push_back(rd32(r->ubuf.data() + r->upos + 4 + l_name));
@@ -284,9 +284,18 @@ static int64_t next_batch_host(fpb_reader *r, uint32_t max_reads, fp_batch_view 
 
 int64_t fpb_next_batch(fpb_reader *r, uint32_t max_reads, fp_batch_view *v) {
     if (!r || !v) return -1;
+    if (r->failed) {  // after an error the undecoded stream and the file position are undefined
+        memset(v, 0, sizeof(*v));
+        r->err = "the reader failed earlier: " + r->failure;
+        return -1;
+    }
     const double t0 = now_s(), read0 = r->stats.seconds_read;
     const int64_t n = next_batch_host(r, max_reads, v);
     r->stats.seconds_decode += (now_s() - t0) - (r->stats.seconds_read - read0);
+    if (n < 0 && r->mode == 1 && !r->failed) {  // (a call in the wrong mode leaves the reader usable)
+        r->failed = true;
+        r->failure = r->err;
+    }
     if (n > 0) {
         r->stats.batches++;
         r->stats.records += uint64_t(n);
@@ -311,14 +320,18 @@ static int64_t next_batch_host(fpb_reader *r, uint32_t max_reads, fp_batch_view 
     while (rec.size() < max_reads) {
         if (r->ubuf.size() - p < 4) {
             const size_t rel = p - r->upos;
-            if (!need(r, rel + 4)) break;
+            const int k = need(r, rel + 4);
+            if (k < 0) return -1;  // (the malformed block's error is kept)
+            if (k == 0) break;
             // need() may have compacted or moved the stream: record offsets are kept relative to upos
             p = r->upos + rel;
         }
         const uint32_t bs = rd32(r->ubuf.data() + p);
         if (r->ubuf.size() - p < 4 + size_t(bs)) {
             const size_t rel = p - r->upos;
-            if (!need(r, rel + 4 + bs)) return fail(r, "truncated BAM record");
+            const int k = need(r, rel + 4 + bs);
+            if (k < 0) return -1;
+            if (k == 0) return fail(r, "truncated BAM record");
             p = r->upos + rel;
         }
         if (bs < 32) return fail(r, "BAM record shorter than its fixed fields");

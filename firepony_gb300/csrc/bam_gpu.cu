@@ -1013,9 +1013,18 @@ static int64_t next_batch_device(fpb_reader *r, uint32_t max_reads, fp_batch_vie
 
 extern "C" int64_t fpb_next_batch_device(fpb_reader *r, uint32_t max_reads, fp_batch_view *v) {
     if (!r || !v) return -1;
+    if (r->failed) {  // after an error the carried stream and the file position are undefined
+        memset(v, 0, sizeof(*v));
+        r->err = "the reader failed earlier: " + r->failure;
+        return -1;
+    }
     const double t0 = now_s(), read0 = r->stats.seconds_read;
     const int64_t n = next_batch_device(r, max_reads, v);
     r->stats.seconds_decode += (now_s() - t0) - (r->stats.seconds_read - read0);
+    if (n < 0 && r->mode == 2 && !r->failed) {  // (a call in the wrong mode leaves the reader usable)
+        r->failed = true;
+        r->failure = r->err;
+    }
     if (n > 0) {
         r->stats.batches++;
         r->stats.records += uint64_t(n);
@@ -1029,7 +1038,11 @@ static int64_t next_batch_device(fpb_reader *r, uint32_t max_reads, fp_batch_vie
     r->mode = 2;
     if (!r->dev) {
         r->dev = new DeviceDecoder();
-        if (!setup(r, r->dev)) return dfail(r, "GPU decoder setup failed");
+        if (!setup(r, r->dev)) {
+            destroy_device_decoder(r->dev);
+            r->dev = nullptr;
+            return dfail(r, "GPU decoder setup failed");
+        }
     }
     DeviceDecoder *d = r->dev;
     if (max_reads == 0) return 0;

@@ -111,6 +111,8 @@ struct fpb_reader {
     fpb_detail::BatchBufs bufs[FPB_BUFFER_SETS];
     int next_set = 0;
     fpb_stats stats{};
+    bool failed = false;  // a batch failed: the stream state is undefined, every later call fails
+    std::string failure;
     int mode = 0;  // 0: no batch yet, 1: host decoding (fpb_next_batch), 2: GPU decoding (fpb_next_batch_device)
     fpb_detail::DeviceDecoder *dev = nullptr;
 };

@@ -97,3 +97,27 @@ def test_bgzf_block_decoder_against_zlib():
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert r.stdout.startswith("ok")
+
+
+def test_corrupt_block_fails_and_stays_failed(data, tmp_path):
+    """A BGZF block with a wrong CRC-32 ends decoding with an error; the reader then refuses further batches
+    (its undecoded stream is undefined after the error) instead of returning later records."""
+    from firepony_gb300 import bam
+    p, ref, batches, path, targets, rg_ids = data
+    raw = bytearray(path.read_bytes())
+    o, blocks = 0, []
+    while o + 18 <= len(raw):
+        n = int.from_bytes(raw[o + 16:o + 18], "little") + 1
+        blocks.append((o, n))
+        o += n
+    o, n = blocks[len(blocks) // 2]
+    raw[o + n - 8] ^= 0x5A  # CRC-32 field of a middle block
+    bad = tmp_path / "crc.bam"
+    bad.write_bytes(bytes(raw))
+    r = bam.BamReader(str(bad), threads=2)
+    with pytest.raises(RuntimeError, match="BGZF"):
+        for _ in r.batches(500):
+            pass
+    with pytest.raises(RuntimeError, match="failed earlier"):
+        r.next_batch(500)
+    r.close()

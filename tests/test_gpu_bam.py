@@ -171,4 +171,6 @@ def test_device_decode_corrupt_block(bam_files, tmp_path, where):
     with pytest.raises(RuntimeError, match="BGZF"):
         for _ in r.batches(100000, device=True):
             pass
+    with pytest.raises(RuntimeError, match="failed earlier"):  # the reader stays failed
+        r.next_batch(100000, device=True)
     r.close()
