@@ -222,6 +222,18 @@ def test_replay_all_reads_exact(native, rpw):
     assert_tables_equal(te, to)
 
 
+def test_replay_all_wide_bands(native):
+    """The uneven-batch workload (bands 16..37) with every BAQ read replayed: the exact FP64 kernels across a
+    warp's lanes (16x3, 32x2 and 32x4 lanes x slots) replace the certified FP32 results of every band class."""
+    from firepony_gb300.abi import FP_FLAG_REPLAY_ALL
+    p, ref, batches = make_dataset("batched_uneven", 6000, 1500, 400_000)
+    te, se, ge = run_engine(ref, batches, p.num_read_groups, "fp32", flags=FP_FLAG_REPLAY_ALL)
+    to, so, go = run_oracle(ref, batches, p.num_read_groups)
+    assert se["baq_reads_by_band"][2] > 0
+    assert_stages_equal(batches[-1], ge, go)
+    assert_tables_equal(te, to)
+
+
 def test_replay_all_edge_cases(native):
     from firepony_gb300.abi import FP_FLAG_REPLAY_ALL
     from tests.edge_cases import edge_case_dataset
