@@ -58,6 +58,7 @@ def parse():
                     help="input batches of the uneven-batch measurement (0: skip)")
     ap.add_argument("--coalesce-reads", type=int, default=1_000_000, help="fp_options.coalesce_reads of its coalesced run")
     ap.add_argument("--serve-jobs", type=int, default=128, help="jobs of the serving measurement (0: skip)")
+    ap.add_argument("--no-refstore", action="store_true", help="skip the reference store start-up measurement")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="job arrivals per second (Poisson)")
     ap.add_argument("--serve-slots", type=int, default=3, help="engines of the job server")
     ap.add_argument("--serve-max-reads", type=int, default=5_000_000, help="largest job (log-uniform from 1000)")
@@ -268,6 +269,63 @@ def run_serving(args):
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "mean_ms": float(lat.mean()), "max_ms": float(lat.max()), "reads": reads, "reads_per_s": reads / span,
             "errors": sum(1 for r in res if r.error)}
+
+
+def run_refstore(args):
+    """Start-up of the resident reference (the serving configuration's 3 contigs / 250 Mbp and 500k known
+    sites): building the store image, publishing it in POSIX shared memory (the preloader), mapping it in a
+    reader, and attaching it to engines (the first attach uploads the image with one copy, later ones share
+    it), against an engine uploading the same contigs and sites for itself (fp_engine_set_contig /
+    fp_engine_set_known_sites). One 20k-read batch through an attached and a self-loaded engine checks that
+    the tables are identical."""
+    import numpy as np
+    import torch
+    from firepony_gb300 import synth
+    from firepony_gb300.engine import Engine
+    from firepony_gb300.refstore import RefStore
+    p = synth.PRESETS["serving_mixed"]
+    t0 = time.perf_counter()
+    ref = synth.Reference(p)
+    gen_s = time.perf_counter() - t0
+    name = f"/fpgb_bench_{os.getpid()}"
+    out = {"reference": "serving_mixed: 3 contigs / 250 Mbp, 450k SNP + 50k indel sites",
+           "generate_ms": gen_s * 1e3}
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, (time.perf_counter() - t) * 1e3
+
+    engines = []
+    store = mapped = None
+    try:
+        store, out["build_ms"] = timed(lambda: RefStore.build(ref))
+        out["image_mb"] = store.info()["image_bytes"] / 1e6
+        _, out["publish_ms"] = timed(lambda: store.publish(name))
+        mapped, out["open_ms"] = timed(lambda: RefStore.open(name))
+        for i in range(3):
+            engines.append(Engine(num_read_groups=p.num_read_groups))
+        _, out["attach_first_ms"] = timed(lambda: engines[0].attach_refstore(mapped))
+        _, out["attach_next_ms"] = timed(lambda: engines[1].attach_refstore(mapped))
+        _, out["engine_upload_ms"] = timed(lambda: engines[2].load_reference(ref))
+        b = ref.batch(0, 20_000)
+        tabs = []
+        for e in (engines[0], engines[2]):
+            e.submit(b)
+            tabs.append(e.finalize())
+        out["tables_identical"] = all(np.array_equal(tabs[0][t][k], tabs[1][t][k]) for t in tabs[0] for k in tabs[0][t])
+    except Exception as ex:  # e.g. a shared-memory mount too small for the image
+        out["error"] = str(ex)
+    finally:
+        for e in engines:
+            e.close()
+        for st in (mapped, store):
+            if st is not None:
+                st.close()
+        RefStore.unlink(name)
+    return out
 
 
 def run_bam(args, res):
@@ -539,6 +597,7 @@ def main():
         bam_in = run_bam(args, res) if args.bam_batches > 0 and world == 1 else None
         batched = run_batched(args) if args.batched_batches > 0 and world == 1 else None
         configs = run_config_legs(args) if args.config_legs and world == 1 else None
+        refstore = run_refstore(args) if not args.no_refstore and world == 1 else None
         line = {"metric": METRIC, "value": value, "unit": "reads/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
@@ -555,6 +614,7 @@ def main():
                 "bam": bam_in,
                 "batched": batched,
                 "configs": configs,
+                "refstore": refstore,
                 "clocks": res["clocks"],
                 "stage_ms": [round(x, 3) for x in res["stage_ms"]],
                 "baq_reads": res["stats"]["baq_reads"],

@@ -1,4 +1,4 @@
-"""ctypes mirrors of the C ABI structs in include/firepony_gb300.h."""
+"""ctypes mirrors of the C ABI structs in include/firepony_gb300.h and include/firepony_gb300_store.h."""
 from __future__ import annotations
 
 import ctypes as C
@@ -46,6 +46,12 @@ class FpStats(C.Structure):
                 ("baq_escalated_by_cause", C.c_uint64 * 2),
                 ("baq_band_cells", C.c_uint64 * 3), ("baq_main_launches", C.c_uint64),
                 ("baq_main_ms", C.c_double), ("baq_path_ms", C.c_double * 4)]
+
+
+class FpRefstoreInfo(C.Structure):
+    _fields_ = [("num_contigs", C.c_uint32), ("attached_engines", C.c_uint32), ("total_bases", C.c_uint64),
+                ("total_sites", C.c_uint64), ("image_bytes", C.c_uint64), ("mapped", C.c_int32),
+                ("device", C.c_int32)]
 
 
 def table_to_numpy(tv: FpTableView) -> dict:

@@ -1,7 +1,7 @@
 """In-tree build of the native libraries.
 
-* ``libfpengine.so`` — the CUDA engine and its C ABI (``include/firepony_gb300.h``), compiled by nvcc for
-  sm_103a only.
+* ``libfpengine.so`` — the CUDA engine and its C ABI (``include/firepony_gb300.h``, and the reference store of
+  ``include/firepony_gb300_store.h``), compiled by nvcc for sm_103a only.
 * ``libfpsynth.so`` — the seeded synthetic-input generator (host C++).
 
 Everything is compiled in parallel into ``firepony_gb300/_build`` (git-ignored). Sources are rebuilt when
@@ -36,6 +36,7 @@ ENGINE_UNITS = [
     ("k_sort.cu", []),
     ("k_post.cu", ["-fmad=false"]),    # empirical quality: exact IEEE double sums and products
     ("report.cpp", []),
+    ("refstore.cu", []),                # reference store: shared-memory segments, one device copy per GPU
 ]
 
 

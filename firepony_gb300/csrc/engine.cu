@@ -17,7 +17,9 @@
 #include <vector>
 
 #include "firepony_gb300.h"
+#include "firepony_gb300_store.h"
 #include "kernels.h"
+#include "refstore_internal.h"
 
 using namespace fpg;
 
@@ -96,6 +98,7 @@ struct fp_engine {
     std::vector<DevBuf> site_bufs;
     DevBuf d_sites;
     DevRef ref{};
+    fp_refstore *store = nullptr;  // when set, `ref` is the store's device copy and the buffers above are empty
 
     // tables
     Tables tables{};
@@ -272,6 +275,7 @@ void fp_engine_destroy(fp_engine *eng) {
     if (eng->st2) cudaStreamSynchronize(eng->st2);
     if (eng->st_copy) cudaStreamSynchronize(eng->st_copy);
     if (eng->st3) cudaStreamSynchronize(eng->st3);
+    if (eng->store) refstore_release(eng->store);
     for (auto &b : eng->contig_bufs) b.release();
     for (auto &b : eng->site_bufs) b.release();
     DevBuf *bufs[] = {&eng->d_contigs, &eng->d_sites, &eng->tab_obs, &eng->tab_mism, &eng->tab_stage, &eng->tab_cyc, &eng->in_bufs[0], &eng->in_bufs[1], &eng->oplen,
@@ -297,6 +301,7 @@ const char *fp_last_error(const fp_engine *eng) { return eng ? eng->err.c_str() 
 
 fp_status fp_engine_set_contig(fp_engine *eng, uint32_t id, const uint32_t *packed4, uint64_t n) {
     if (!eng || (!packed4 && n)) return FP_BAD_INPUT;
+    if (eng->store) return eng->fail(FP_BAD_INPUT, "the engine reads an attached reference store");
     CK(cudaSetDevice(eng->device), "set device");
     if (id >= eng->h_contigs.size()) {
         eng->h_contigs.resize(id + 1, DevContig{nullptr, 0});
@@ -322,6 +327,7 @@ fp_status fp_engine_set_contig(fp_engine *eng, uint32_t id, const uint32_t *pack
 fp_status fp_engine_set_known_sites(fp_engine *eng, uint32_t id, const uint32_t *start, const uint32_t *stop,
                                     uint32_t n) {
     if (!eng || ((!start || !stop) && n)) return FP_BAD_INPUT;
+    if (eng->store) return eng->fail(FP_BAD_INPUT, "the engine reads an attached reference store");
     CK(cudaSetDevice(eng->device), "set device");
     if (id >= eng->h_sites.size()) {
         eng->h_sites.resize(id + 1, DevSites{nullptr, nullptr, nullptr, 0, 0});
@@ -343,6 +349,42 @@ fp_status fp_engine_set_known_sites(fp_engine *eng, uint32_t id, const uint32_t 
         CK(cudaMemcpy(p + 2 * size_t(n), maxend.data(), n * 4, cudaMemcpyHostToDevice), "known-site upload");
     }
     eng->h_sites[id] = DevSites{p, p + n, p + 2 * size_t(n), n, 0};
+    return upload_refs(eng);
+}
+
+static fp_status co_flush(fp_engine *eng);
+
+// Engines of one GPU share a reference store's device copy (segmented_database.h:224-244 keeps one resident
+// set per engine). The engine's own contigs and sites are freed; work already queued is finished first, and
+// host batches staged for coalescing are submitted under the reference they were staged with.
+fp_status fp_engine_attach_refstore(fp_engine *eng, fp_refstore *store) {
+    if (!eng) return FP_BAD_INPUT;
+    if (store == eng->store) return FP_OK;
+    CK(cudaSetDevice(eng->device), "set device");
+    const fp_status fs = co_flush(eng);
+    if (fs != FP_OK) return fs;
+    cudaStream_t sts[] = {eng->st, eng->st2, eng->st3, eng->st_copy};
+    for (cudaStream_t x : sts)
+        if (x) CK(cudaStreamSynchronize(x), "attach reference store");
+    const DevRef *r = nullptr;
+    if (store) {
+        std::string m;
+        int status = FP_OK;
+        r = refstore_acquire(store, eng->device, m, status);
+        if (!r) return eng->fail(fp_status(status), m);
+    }
+    if (eng->store) refstore_release(eng->store);
+    for (auto &b : eng->contig_bufs) b.release();
+    for (auto &b : eng->site_bufs) b.release();
+    eng->contig_bufs.clear();
+    eng->site_bufs.clear();
+    eng->h_contigs.clear();
+    eng->h_sites.clear();
+    eng->store = store;
+    if (store) {
+        eng->ref = *r;
+        return FP_OK;
+    }
     return upload_refs(eng);
 }
 

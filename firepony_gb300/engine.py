@@ -10,8 +10,8 @@ from pathlib import Path
 
 import numpy as np
 
-from .abi import (FP_OK, STATUS_NAMES, FpBatchView, FpOptions, FpStats, FpTableView, FP_BAQ_FP32, FP_BAQ_FP64,
-                  table_to_numpy)
+from .abi import (FP_OK, STATUS_NAMES, FpBatchView, FpOptions, FpRefstoreInfo, FpStats, FpTableView, FP_BAQ_FP32,
+                  FP_BAQ_FP64, table_to_numpy)
 
 _BUILD = Path(__file__).resolve().parent / "_build"
 _lib = None
@@ -66,6 +66,24 @@ def lib():
         L.fp_sort_entries_static.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_int, C.c_void_p]
         L.fp_host_alloc.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
         L.fp_host_free.argtypes = [C.c_void_p]
+        # reference store (include/firepony_gb300_store.h)
+        L.fp_refstore_create.argtypes = [C.c_uint32, C.POINTER(C.c_void_p)]
+        L.fp_refstore_set_contig.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint64]
+        L.fp_refstore_set_known_sites.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32]
+        L.fp_refstore_shm_name.argtypes = [C.c_char_p, C.c_char_p, C.c_size_t]
+        L.fp_refstore_publish.argtypes = [C.c_void_p, C.c_char_p]
+        L.fp_refstore_open.argtypes = [C.c_char_p, C.POINTER(C.c_void_p)]
+        L.fp_refstore_unlink.argtypes = [C.c_char_p]
+        L.fp_refstore_get_info.argtypes = [C.c_void_p, C.POINTER(FpRefstoreInfo)]
+        L.fp_refstore_get_contig.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(C.POINTER(C.c_uint32)),
+                                             C.POINTER(C.c_uint64)]
+        L.fp_refstore_get_known_sites.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(C.POINTER(C.c_uint32)),
+                                                  C.POINTER(C.POINTER(C.c_uint32)), C.POINTER(C.c_uint32)]
+        L.fp_refstore_upload.argtypes = [C.c_void_p, C.c_int]
+        L.fp_engine_attach_refstore.argtypes = [C.c_void_p, C.c_void_p]
+        L.fp_refstore_destroy.argtypes = [C.c_void_p]
+        L.fp_refstore_last_error.restype = C.c_char_p
+        L.fp_refstore_last_error.argtypes = [C.c_void_p]
         _lib = L
     return _lib
 
@@ -133,6 +151,7 @@ class Engine:
         if getattr(self, "h", None):
             lib().fp_engine_destroy(self.h)
             self.h = None
+        self._store = None
 
     def __del__(self):
         try:
@@ -143,6 +162,13 @@ class Engine:
     def set_contig(self, cid: int, words: np.ndarray, n: int):
         w = np.ascontiguousarray(words, dtype=np.uint32)
         self._check(lib().fp_engine_set_contig(self.h, cid, w.ctypes.data, n), "set_contig")
+
+    def attach_refstore(self, store):
+        """Reads contigs and known sites from `store`'s device copy (fp_engine_attach_refstore; uploaded to this
+        engine's GPU first if needed). None detaches. The store stays referenced while attached."""
+        self._check(lib().fp_engine_attach_refstore(self.h, store.h if store is not None else None),
+                    "attach_refstore")
+        self._store = store
 
     def set_known_sites(self, cid: int, start: np.ndarray, stop: np.ndarray):
         st = np.ascontiguousarray(start, dtype=np.uint32)

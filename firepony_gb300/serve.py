@@ -2,8 +2,10 @@
 
 The reference runs one job per process (firepony.cu:300-420): it loads the reference and known sites,
 streams the job's batches through its pipelines and writes the report. A service answering many jobs
-keeps that state resident instead. `JobServer` holds `slots` engines (`fp_engine`), each with the
-reference contigs and known sites uploaded once, and a worker thread per engine that takes jobs from one
+keeps that state resident instead. `JobServer` holds `slots` engines (`fp_engine`) that all read one device
+copy of the reference contigs and known sites (a reference store, include/firepony_gb300_store.h: given as
+a `RefStore`, e.g. one a preloader published in shared memory, or built from `reference`), and a worker
+thread per engine that takes jobs from one
 FIFO queue: `fp_engine_reset` (tables to zero, residency kept), the job's batches through
 `fp_engine_submit_batch` (host buffers, copies included; each next batch's copy is queued with
 `fp_engine_prefetch_batch` while the current one runs), `fp_engine_finalize`. Engines run on their own
@@ -29,6 +31,7 @@ from typing import Callable, Iterable
 import numpy as np
 
 from .engine import Engine
+from .refstore import RefStore
 
 
 def estimate_job_bytes(max_batch_reads: int, mean_read_len: float = 151.0) -> int:
@@ -78,17 +81,28 @@ class _Pending:
 
 class JobServer:
     def __init__(self, reference, num_read_groups: int, slots: int = 2, baq_mode: str = "fp32", device: int = 0,
-                 keep_tables: bool = False, hbm_budget_bytes: int | None = None, engine_factory=None):
+                 keep_tables: bool = False, hbm_budget_bytes: int | None = None, engine_factory=None,
+                 share_reference: bool = True):
+        """reference: a RefStore (attached by every engine), or contigs/sites (a synth.Reference) from which
+        the server builds one store (share_reference) or which every engine uploads for itself."""
         self.keep_tables = keep_tables
         self.hbm_budget = hbm_budget_bytes
         self.engines = []
+        self._own_store = None
+        store = reference if isinstance(reference, RefStore) else None
+        if store is None and share_reference and engine_factory is None:
+            store = self._own_store = RefStore.build(reference)
         for _ in range(slots):
             if engine_factory is not None:
                 e = engine_factory()
             else:
                 e = Engine(num_read_groups=num_read_groups, baq_mode=baq_mode, device=device)
-                e.load_reference(reference)
+                if store is not None:
+                    e.attach_refstore(store)
+                else:
+                    e.load_reference(reference)
             self.engines.append(e)
+        self.store = store
         self._cv = threading.Condition()
         self._queue: deque = deque()
         self._closing = False
@@ -164,6 +178,9 @@ class JobServer:
         for e in self.engines:
             e.close()
         self.engines = []
+        if self._own_store is not None:
+            self._own_store.close()
+            self._own_store = None
 
 
 def poisson_schedule(num_jobs: int, rate_per_s: float, min_reads: int, max_reads: int, seed: int):
