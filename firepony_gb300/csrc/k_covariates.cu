@@ -28,6 +28,7 @@ struct CovSmem {
 struct FracSmem {
     u32 pre[512];   // window-relative prefix counts of the SNP / insertion / deletion bits (10 bits each)
     i16 last[512];  // last base before j (window-relative) whose BQ tag is NO_BAQ_UNCERTAINTY, or -1
+    u8 nz[512];     // read position -> which of the base's three fractional errors are nonzero (bits M, I, D)
 };
 
 // calculateFractionalErrorArray (device/fractional_errors.cu:39-141) for the three error bits at once, in
@@ -90,6 +91,7 @@ __device__ void fractional_errors_warp(const CovSmem &sm, FracSmem &fs, u32 wx, 
                 o[0] = (bfv & BF_SNP) ? 1.0f : 0.0f;
                 o[1] = (bfv & BF_INS) ? 1.0f : 0.0f;
                 o[2] = (bfv & BF_DEL) ? 1.0f : 0.0f;
+                fs.nz[wx + j] = u8(((bfv & BF_SNP) ? 1 : 0) | ((bfv & BF_INS) ? 2 : 0) | ((bfv & BF_DEL) ? 4 : 0));
             } else {
                 // float(double(n) / double(len)) as in the reference, computed as one correctly rounded FP32
                 // division: with n <= 2^24 and len < 2^28 the exact quotient is at least 2^-25/len away from any
@@ -100,6 +102,8 @@ __device__ void fractional_errors_warp(const CovSmem &sm, FracSmem &fs, u32 wx, 
                 o[0] = __fdiv_rn(float(d & 1023u), len);
                 o[1] = __fdiv_rn(float((d >> 10) & 1023u), len);
                 o[2] = __fdiv_rn(float(d >> 20), len);
+                // a nonzero count over a range of at most 512 bases gives a nonzero float quotient
+                fs.nz[wx + j] = u8(((d & 1023u) ? 1 : 0) | (((d >> 10) & 1023u) ? 2 : 0) | ((d >> 20) ? 4 : 0));
             }
         }
         if (m6) carry_next = c + __ffs(m6) - 1;
@@ -254,9 +258,17 @@ __global__ void __launch_bounds__(COV_WARPS * 32) k_cov(DevBatch b, BatchWork w,
                 sub = res;
                 ind = (i < 4 || i > readLength - 5) ? CYCLE_INVALID : res;
                 context_keys_smem(sm.sym, neg, hq, off, cm, ci);
-                mm0 = frac[size_t(off) * 3 + 0];
-                mm1 = frac[size_t(off) * 3 + 1];
-                mm2 = frac[size_t(off) * 3 + 2];
+                if (EMIT) {
+                    mm0 = frac[size_t(off) * 3 + 0];
+                    mm1 = frac[size_t(off) * 3 + 1];
+                    mm2 = frac[size_t(off) * 3 + 2];
+                } else {
+                    // the count pass needs only which values are nonzero (the fractional-error step's mask)
+                    const u8 z = fs.nz[off];
+                    mm0 = (z & 1) ? 1.f : 0.f;
+                    mm1 = (z & 2) ? 1.f : 0.f;
+                    mm2 = (z & 4) ? 1.f : 0.f;
+                }
             }
             const u32 kq0 = ks.qual_base + (rgq + qm) * EV_SLOTS + 0;
             const u32 kq1 = ks.qual_base + (rgq + 45) * EV_SLOTS + 2;
@@ -313,12 +325,17 @@ __global__ void __launch_bounds__(COV_WARPS * 32) k_cov(DevBatch b, BatchWork w,
                 if (mm2 != 0.f) cnt += 1 + (vci ? 1 : 0) + (vxi ? 1 : 0);
             }
             u32 x = cnt;
+            u32 chunk_total;
+            if (EMIT) {
 #pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const u32 y = __shfl_up_sync(FULL, x, d);
-                if (lane >= d) x += y;
+                for (int d = 1; d < 32; d <<= 1) {
+                    const u32 y = __shfl_up_sync(FULL, x, d);
+                    if (lane >= d) x += y;
+                }
+                chunk_total = __shfl_sync(FULL, x, 31);
+            } else {
+                chunk_total = __reduce_add_sync(FULL, cnt);  // the count pass needs the total only
             }
-            const u32 chunk_total = __shfl_sync(FULL, x, 31);
             if (EMIT && cnt) {
                 u64 *o = out + nnz_total + (x - cnt);
                 u32 j = 0;

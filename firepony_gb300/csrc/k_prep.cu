@@ -637,7 +637,7 @@ __global__ void __launch_bounds__(PREP_WARPS * 32) k_prep(DevBatch b, DevRef ref
 // original quality per I base. In FP32 mode (exact == 0) the HMM outputs can be undecided (baq_amb); if a
 // capped value depends on one (an undecided quality of a base whose state is the match at its expected
 // position, or an undecided state whose candidates do not all give MIN_BASE_QUAL), the read goes to the
-// escalation list and nothing is written.
+// escalation list and the exact replay's capping rewrites its values.
 __global__ void __launch_bounds__(64) k_cap(DevBatch b, BatchWork w, const u32 *list, const u32 *count, int exact) {
     constexpr u32 FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -663,7 +663,7 @@ __global__ void __launch_bounds__(64) k_cap(DevBatch b, BatchWork w, const u32 *
         }
         const i16 refOffset = i16(int(hw.x) - int(rw.x) + int(reference_shift));
 
-        // baq_start: first event with a read coordinate >= window.x; end: first later event past window.y
+        // baq_start: first event with a read coordinate >= window.x
         u32 baq_start = 0;
         for (u32 c = 0; c < n; c += 32) {
             const u32 i = c + lane;
@@ -671,35 +671,42 @@ __global__ void __launch_bounds__(64) k_cap(DevBatch b, BatchWork w, const u32 *
             const u32 m = __ballot_sync(FULL, rb != U16_NONE && rb >= wcl.x);
             if (m) { baq_start = c + __ffs(m) - 1; break; }
         }
-        u32 end = n;
-        for (u32 c = baq_start; c < n; c += 32) {
-            const u32 i = c + lane;
-            const u16 rb = i < n ? u16(rc[i] & 0xFFFF) : U16_NONE;
-            const u32 m = __ballot_sync(FULL, rb != U16_NONE && rb > wcl.y);
-            if (m) { end = c + __ffs(m) - 1; break; }
-        }
 
-        // pass 1: read-step total (cap_baq<false>) and, in FP32 mode, whether any capped value is undecided
-        u32 readI_total = 0, refI_c = 0, numD_c = 0, readI_c = 0;
+        // One walk from baq_start to `end`, the first later event past window.y (found in the chunk that holds
+        // it, which ends the walk). It makes the read-step total of cap_baq<false>, and writes cap_baq<true>'s
+        // values already recoded (recode_baq_qualities: quality + 64 - capped; an I base's capped value is its
+        // quality, so its tag is 64). Bases the walk does not write keep the batch's 0xFF, which recoding
+        // leaves alone. The writes are speculative in FP32 mode: a read whose capped values depend on an
+        // undecided HMM output is deferred, and the exact replay's capping rewrites the same bases (the
+        // walk does not depend on the HMM) before anything reads them.
+        u32 end = n;
+        u32 refI_c = 0, numD_c = 0, readI_c = 0;
         bool escalate = false, by_state = false;
         for (u32 c = baq_start; c < end; c += 32) {
             const u32 i = c + lane;
+            const u32 rcv = i < end ? rc[i] : u32(U16_NONE);
+            const u16 rb = u16(rcv & 0xFFFF);
+            const u32 past = __ballot_sync(FULL, rb != U16_NONE && rb > wcl.y);
+            if (past) end = c + __ffs(past) - 1;
             const bool in = i < end;
             const u8 t = in ? ty[i] : EV_S;
             const bool isM = in && t == EV_M, isI = in && t == EV_I, isD = in && t == EV_D;
             const bool isRef = in && (t == EV_S || t == EV_D || t == EV_M);
             const u32 mRef = __ballot_sync(FULL, isRef), mD = __ballot_sync(FULL, isD);
             const u32 mRead = __ballot_sync(FULL, isM || isI);
-            if (!exact && isM) {
+            if (isI) {
+                w.tag[qs + rb] = NO_BAQ_UNCERTAINTY;
+            } else if (isM) {
                 const u32 refI = refI_c + __popc(mRef & lt), numD = numD_c + __popc(mD & lt);
                 const u32 readI = readI_c + __popc(mRead & lt);
-                const u16 rb = u16(rc[i] & 0xFFFF);
-                const u8 amb = w.baq_amb[qs + rb];
-                if (amb) {
-                    const u32 expectedPos = refI - u32(int(refOffset)) + (i - numD - baq_start - readI) + u32(int(read_shift));
-                    const u32 state = w.baq_state[qs + rb];
-                    // the capped value uses the HMM quality only when the MAP state is the match at expectedPos
-                    const bool at_expected = (state & 3) == 0 && (state >> 2) == expectedPos;
+                const u32 expectedPos = refI - u32(int(refOffset)) + (i - numD - baq_start - readI) + u32(int(read_shift));
+                const u32 state = w.baq_state[qs + rb];
+                const u8 oq = b.quals[qs + rb];
+                const u8 bq = w.baq_q[qs + rb];
+                // the capped value uses the HMM quality only when the MAP state is the match at expectedPos
+                const bool at_expected = (state & 3) == 0 && (state >> 2) == expectedPos;
+                if (!exact) {
+                    const u8 amb = w.baq_amb[qs + rb];
                     if (amb & 4) {
                         escalate = true;
                         by_state = true;
@@ -716,14 +723,21 @@ __global__ void __launch_bounds__(64) k_cap(DevBatch b, BatchWork w, const u32 *
                         escalate = true;
                     }
                 }
+                const u8 v = at_expected ? (bq < oq ? bq : oq) : u8(MIN_BASE_QUAL);
+                w.tag[qs + rb] = u8(u8(oq + 64) - v);
             }
             refI_c += __popc(mRef);
             numD_c += __popc(mD);
             readI_c += __popc(mRead);
         }
-        readI_total = readI_c;
-        const bool need_update = readI_total == u32(wcl.y - wcl.x + 1);
-        if (need_update && !exact && __any_sync(FULL, escalate)) {
+        const bool need_update = readI_c == u32(wcl.y - wcl.x + 1);
+        if (!need_update) {
+            // cap_baq<true> is skipped: the window keeps its original qualities, recoded to 64
+            __syncwarp();
+            for (u32 i = wcl.x + lane; i <= wcl.y; i += 32) w.tag[qs + i] = NO_BAQ_UNCERTAINTY;
+            continue;
+        }
+        if (!exact && __any_sync(FULL, escalate)) {
             if (lane == 0) {
                 // escalation lists by band class: class 0 (band <= 7), class 1 (band <= 15), class 2 (wider)
                 const u32 cls = w.bw[r] <= 7 ? 0 : (w.bw[r] <= 15 ? 1 : 2);
@@ -734,46 +748,6 @@ __global__ void __launch_bounds__(64) k_cap(DevBatch b, BatchWork w, const u32 *
             // escalation cause: some MAP state undecided, or only qualities undecided
             const bool st = __any_sync(FULL, by_state);
             if (lane == 0) atomicAdd(&w.counters[st ? 22 : 23], 1u);
-            continue;
-        }
-        if (need_update) {
-            refI_c = numD_c = readI_c = 0;
-            for (u32 c = baq_start; c < end; c += 32) {
-                const u32 i = c + lane;
-                const bool in = i < end;
-                const u8 t = in ? ty[i] : EV_S;
-                const bool isM = in && t == EV_M, isI = in && t == EV_I, isD = in && t == EV_D;
-                const bool isRef = in && (t == EV_S || t == EV_D || t == EV_M);
-                const u32 mRef = __ballot_sync(FULL, isRef), mD = __ballot_sync(FULL, isD);
-                const u32 mRead = __ballot_sync(FULL, isM || isI);
-                if (isI) {
-                    const u16 rb = u16(rc[i] & 0xFFFF);
-                    w.tag[qs + rb] = b.quals[qs + rb];
-                } else if (isM) {
-                    const u32 refI = refI_c + __popc(mRef & lt), numD = numD_c + __popc(mD & lt);
-                    const u32 readI = readI_c + __popc(mRead & lt);
-                    const u16 rb = u16(rc[i] & 0xFFFF);
-                    const u32 expectedPos = refI - u32(int(refOffset)) + (i - numD - baq_start - readI) + u32(int(read_shift));
-                    const u8 oq = b.quals[qs + rb];
-                    const u8 bq = w.baq_q[qs + rb];
-                    const u32 state = w.baq_state[qs + rb];
-                    const bool isIndel = (state & 3) != 0;
-                    w.tag[qs + rb] = (isIndel || (state >> 2) != expectedPos) ? u8(MIN_BASE_QUAL) : (bq < oq ? bq : oq);
-                }
-                refI_c += __popc(mRef);
-                numD_c += __popc(mD);
-                readI_c += __popc(mRead);
-            }
-        } else {
-            for (u32 i = wcl.x + lane; i <= wcl.y; i += 32) w.tag[qs + i] = b.quals[qs + i];
-        }
-        __syncwarp();
-        // recode_baq_qualities (device/baq.cu:1058-1081)
-        const u32 ql = b.qual_len[r];
-        for (u32 i = lane; i < ql; i += 32) {
-            const u8 v = w.tag[qs + i];
-            if (v == 0xFF) continue;
-            w.tag[qs + i] = u8(u8(b.quals[qs + i] + 64) - v);
         }
     }
 }
