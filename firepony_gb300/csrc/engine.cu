@@ -86,6 +86,11 @@ struct fp_engine {
     cudaStream_t st = nullptr;
     cudaStream_t st2 = nullptr;          // band-class-1 BAQ, concurrent with class 0
     cudaStream_t st3 = nullptr;          // first covariate count pass, concurrent with the FP64 replays
+    // sort + ordered fold of a batch's entries: in batch order on its own stream, beside the next batch's
+    // copies and preparation. fold_end marks the last queued fold; its timing is read once it has finished.
+    cudaStream_t st_fold = nullptr;
+    cudaEvent_t fold_start = nullptr, fold_end = nullptr;
+    bool fold_pending = false;
     cudaEvent_t fork = nullptr, join = nullptr, cov1_done = nullptr;
     std::string err;
     bool finalized = false;
@@ -178,6 +183,18 @@ fp_status alloc_tables(fp_engine *eng) {
     return FP_OK;
 }
 
+// Waits for the last queued sort + fold and adds its device time to the statistics.
+cudaError_t fold_harvest(fp_engine *eng) {
+    if (!eng->fold_pending) return cudaSuccess;
+    const cudaError_t e = cudaEventSynchronize(eng->fold_end);
+    if (e != cudaSuccess) return e;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, eng->fold_start, eng->fold_end) == cudaSuccess)
+        eng->stats.gpu_ms_per_stage[FP_STAGE_SORT_REDUCE] += ms;
+    eng->fold_pending = false;
+    return cudaSuccess;
+}
+
 fp_status upload_refs(fp_engine *eng) {
     CK(eng->d_contigs.ensure(std::max<size_t>(1, eng->h_contigs.size()) * sizeof(DevContig)), "contig table");
     if (!eng->h_contigs.empty())
@@ -225,6 +242,9 @@ fp_status fp_engine_create(const fp_options *o, fp_engine **out) {
     }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&eng->st_copy, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&eng->st3, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&eng->st_fold, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&eng->fold_start);
+    if (e == cudaSuccess) e = cudaEventCreate(&eng->fold_end);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&eng->cov1_done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&eng->in_ev[0], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&eng->in_ev[1], cudaEventDisableTiming);
@@ -275,6 +295,7 @@ void fp_engine_destroy(fp_engine *eng) {
     if (eng->st2) cudaStreamSynchronize(eng->st2);
     if (eng->st_copy) cudaStreamSynchronize(eng->st_copy);
     if (eng->st3) cudaStreamSynchronize(eng->st3);
+    if (eng->st_fold) cudaStreamSynchronize(eng->st_fold);
     if (eng->store) refstore_release(eng->store);
     for (auto &b : eng->contig_bufs) b.release();
     for (auto &b : eng->site_bufs) b.release();
@@ -291,6 +312,9 @@ void fp_engine_destroy(fp_engine *eng) {
     if (eng->st_copy) cudaStreamDestroy(eng->st_copy);
     if (eng->st3) cudaStreamDestroy(eng->st3);
     if (eng->cov1_done) cudaEventDestroy(eng->cov1_done);
+    if (eng->st_fold) cudaStreamDestroy(eng->st_fold);
+    if (eng->fold_start) cudaEventDestroy(eng->fold_start);
+    if (eng->fold_end) cudaEventDestroy(eng->fold_end);
     for (auto &x : eng->in_ev)
         if (x) cudaEventDestroy(x);
     if (eng->st) cudaStreamDestroy(eng->st);
@@ -363,7 +387,7 @@ fp_status fp_engine_attach_refstore(fp_engine *eng, fp_refstore *store) {
     CK(cudaSetDevice(eng->device), "set device");
     const fp_status fs = co_flush(eng);
     if (fs != FP_OK) return fs;
-    cudaStream_t sts[] = {eng->st, eng->st2, eng->st3, eng->st_copy};
+    cudaStream_t sts[] = {eng->st, eng->st2, eng->st3, eng->st_copy, eng->st_fold};
     for (cudaStream_t x : sts)
         if (x) CK(cudaStreamSynchronize(x), "attach reference store");
     const DevRef *r = nullptr;
@@ -780,22 +804,35 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
     CK(cudaMemcpyAsync(&esc2, w.counters + 27, 4, cudaMemcpyDeviceToHost, st), "D2H");
     CK(cudaStreamSynchronize(st), "covariates");
     const u64 N = tail[0];
+    const size_t sort_bytes = std::max(radix_tmp_bytes(N), fold_tmp_bytes(N));
+    // the previous batch's sort + fold may still read the entry buffers and their scratch: growing them waits
+    // for it; otherwise the emit below waits for it on the device
+    if (eng->entries.cap < al(N * 8 + 8) || eng->entries_alt.cap < al(N * 8 + 8) || eng->sort_tmp.cap < sort_bytes)
+        CK(fold_harvest(eng), "sort + fold");
     CK(eng->entries.ensure(al(N * 8 + 8)), "entries");
     CK(eng->entries_alt.ensure(al(N * 8 + 8)), "entries");
     w.entries = eng->entries.as<u64>();
     w.entries_alt = eng->entries_alt.as<u64>();
-    CK(eng->sort_tmp.ensure(std::max(radix_tmp_bytes(N), fold_tmp_bytes(N))), "sort scratch");
+    CK(eng->sort_tmp.ensure(sort_bytes), "sort scratch");
+    if (eng->fold_pending) CK(cudaStreamWaitEvent(st, eng->fold_end, 0), "fold wait");
     launch_cov_emit(b, w, eng->tables, st);
     CK(cudaGetLastError(), "covariate launch");
     cudaEventRecord(eng->ev[5], st);
 
-    // ---- K4 sort + ordered fold ----
+    // ---- K4 sort + ordered fold, on the fold stream: batches fold in submission order there, and the next
+    // batch's copies and preparation run beside it ----
+    CK(fold_harvest(eng), "sort + fold");  // the previous fold's events are read before they are recorded again
+    CK(cudaStreamWaitEvent(eng->st_fold, eng->ev[5], 0), "fold fork");
+    cudaEventRecord(eng->fold_start, eng->st_fold);
     int key_bits = 1;
     while (key_bits < 32 && (1ull << key_bits) < eng->tables.ks.total) key_bits++;
     u64 *sorted = w.entries;
-    launch_radix_sort(w.entries, w.entries_alt, N, key_bits, eng->sort_tmp.p, eng->sort_tmp.cap, &sorted, st);
-    launch_fold(sorted, N, eng->tables.mism, eng->sort_tmp.p, st);
+    launch_radix_sort(w.entries, w.entries_alt, N, key_bits, eng->sort_tmp.p, eng->sort_tmp.cap, &sorted,
+                      eng->st_fold);
+    launch_fold(sorted, N, eng->tables.mism, eng->sort_tmp.p, eng->st_fold);
     CK(cudaGetLastError(), "sort launch");
+    CK(cudaEventRecord(eng->fold_end, eng->st_fold), "fold join");
+    eng->fold_pending = true;
     cudaEventRecord(eng->ev[6], st);
     u32 dev_err = 0;
     unsigned long long cells[3] = {0, 0, 0};
@@ -808,9 +845,9 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
     if (dev_err & (ERR_INTERNAL | ERR_TIMEOUT | ERR_CAPACITY))
         return eng->fail(FP_DEVICE_ERROR, "kernel reported an internal error status");
     float ms;
-    const int stage_of[6] = {FP_STAGE_H2D, FP_STAGE_OTHER, FP_STAGE_PREP, FP_STAGE_BAQ, FP_STAGE_COVARIATES,
-                             FP_STAGE_SORT_REDUCE};
-    for (int i = 0; i < 6; i++) {
+    // (the sort + fold stage is timed on its own stream, fold_harvest)
+    const int stage_of[5] = {FP_STAGE_H2D, FP_STAGE_OTHER, FP_STAGE_PREP, FP_STAGE_BAQ, FP_STAGE_COVARIATES};
+    for (int i = 0; i < 5; i++) {
         if (cudaEventElapsedTime(&ms, eng->ev[i], eng->ev[i + 1]) == cudaSuccess)
             eng->stats.gpu_ms_per_stage[stage_of[i]] += ms;
     }
@@ -978,6 +1015,7 @@ fp_status fp_engine_finalize(fp_engine *eng) {
         if (s0 != FP_OK) return s0;
     }
     cudaStream_t st = eng->st;
+    CK(fold_harvest(eng), "sort + fold");
     cudaEventRecord(eng->ev[7], st);
     const KeySpace ks = eng->tables.ks;
     const u32 T = ks.total;
@@ -1142,6 +1180,7 @@ fp_status fp_engine_write_report(fp_engine *eng, const char *path, const char *c
 fp_status fp_engine_reset(fp_engine *eng) {
     if (!eng) return FP_BAD_INPUT;
     CK(cudaSetDevice(eng->device), "set device");
+    CK(fold_harvest(eng), "sort + fold");
     const size_t n = eng->tables.ks.total;
     CK(cudaMemsetAsync(eng->tab_obs.p, 0, n * sizeof(unsigned long long), eng->st), "reset");
     CK(cudaMemsetAsync(eng->tab_mism.p, 0, n * sizeof(float), eng->st), "reset");
