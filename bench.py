@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--coalesce-reads", type=int, default=1_000_000, help="fp_options.coalesce_reads of its coalesced run")
     ap.add_argument("--serve-jobs", type=int, default=128, help="jobs of the serving measurement (0: skip)")
     ap.add_argument("--no-refstore", action="store_true", help="skip the reference store start-up measurement")
+    ap.add_argument("--sort-entries", type=int, default=64_000_000, help="entries of the radix sort measurement (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="job arrivals per second (Poisson)")
     ap.add_argument("--serve-slots", type=int, default=3, help="engines of the job server")
     ap.add_argument("--serve-max-reads", type=int, default=5_000_000, help="largest job (log-uniform from 1000)")
@@ -152,8 +153,9 @@ def run_batched(args):
     """The uneven-batch workload (4 contigs / 100 Mbp, reads of 36-250 bp mixed, 0-8 indels per read, 10% wide
     deletions, 16 read groups) as a bounded sample of its many small input batches (sizes uniform in 2k-40k
     reads), from page-locked host buffers through the C ABI: each batch processed alone, then with the engine
-    coalescing them (fp_options.coalesce_reads) into device batches. Wall clock from the first submit to the
-    finished tables; both runs must give identical tables."""
+    coalescing them (fp_options.coalesce_reads) into device batches, and the plain FP64 path on the same
+    coalesced batches. Wall clock from the first submit to the finished tables; all runs must give identical
+    tables."""
     import numpy as np
     from firepony_gb300 import synth
     from firepony_gb300.engine import Engine, PinnedBatch
@@ -166,8 +168,10 @@ def run_batched(args):
     reads = int(sizes.sum())
     out = {}
     tables = {}
-    for name, coalesce in (("per_batch", 0), ("coalesced", args.coalesce_reads)):
-        eng = Engine(num_read_groups=p.num_read_groups, coalesce_reads=coalesce)
+    # the plain path (every BAQ read in exact FP64) on the same coalesced device batches
+    for name, coalesce, mode in (("per_batch", 0, "fp32"), ("coalesced", args.coalesce_reads, "fp32"),
+                                 ("plain_fp64_coalesced", args.coalesce_reads, "fp64")):
+        eng = Engine(num_read_groups=p.num_read_groups, coalesce_reads=coalesce, baq_mode=mode)
         eng.load_reference(ref)
         eng.submit_pipelined([pb.batch for pb in pinned[:4]])  # warm-up
         eng.finalize()
@@ -179,14 +183,16 @@ def run_batched(args):
         dt = time.perf_counter() - t0
         out[name + "_reads_per_s"] = reads / dt
         eng.close()
-    same = all(np.array_equal(tables["per_batch"][t][k], tables["coalesced"][t][k])
-               for t in tables["per_batch"] for k in tables["per_batch"][t])
+    same = all(np.array_equal(tables["per_batch"][t][k], tables[other][t][k])
+               for other in ("coalesced", "plain_fp64_coalesced") for t in tables["per_batch"] for k in tables["per_batch"][t])
     if not args.no_cpu_baseline:
         out["cpu_oracle"] = cpu_baseline(ref, batches, args.cpu_sample_seconds / 3)
     return {"workload": "batched_uneven: 4 contigs / 100 Mbp, reads of 36/76/101/151/250 bp, 0-8 indels per read, "
                         "10% wide deletions, 16 read groups",
             "batches": len(sizes), "reads": reads, "batch_reads": "uniform 2000-40000", "coalesce_reads": args.coalesce_reads,
-            **out, "speedup": out["coalesced_reads_per_s"] / out["per_batch_reads_per_s"], "tables_identical": bool(same),
+            **out, "speedup": out["coalesced_reads_per_s"] / out["per_batch_reads_per_s"],
+            "vs_plain_fp64": out["coalesced_reads_per_s"] / out["plain_fp64_coalesced_reads_per_s"],
+            "tables_identical": bool(same),
             "inputs": "page-locked host buffers through fp_engine_submit_batch (copies in the timed region)"}
 
 
@@ -269,6 +275,52 @@ def run_serving(args):
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "mean_ms": float(lat.mean()), "max_ms": float(lat.max()), "reads": reads, "reads_per_s": reads / span,
             "errors": sum(1 for r in res if r.error)}
+
+
+def _measured_peak_gbs() -> float:
+    """The measured HBM copy bandwidth (MEASURED_PEAKS.json), else the fallback 6800 GB/s."""
+    try:
+        return float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("hbm_gbs", 6800.0))
+    except Exception:
+        return 6800.0
+
+
+def run_sort(args):
+    """The radix sort primitive (fp_sort_entries: stable LSD passes of 8-bit digits over packed 64-bit entries,
+    dense key in the high 32 bits) on `--sort-entries` random entries with 29-bit keys (the context table's key
+    width), inputs in HBM and larger than L2. Algorithmic bytes = entries x 8 B x 2 (read + write) x passes
+    (the histogram reads are not counted), against the measured HBM copy bandwidth. CUDA events on the stream
+    the sort is launched on; the result is checked for sortedness and for being a permutation."""
+    import numpy as np
+    import torch
+    from firepony_gb300.engine import sort_entries
+    n, key_bits = args.sort_entries, 29
+    g = torch.Generator(device="cuda").manual_seed(7)
+    keys = torch.randint(0, 1 << key_bits, (n,), device="cuda", dtype=torch.int64, generator=g)
+    vals = torch.randint(0, 1 << 31, (n,), device="cuda", dtype=torch.int64, generator=g)
+    src = (keys << 32) | vals
+    dst = torch.empty_like(src)
+    stream = torch.cuda.current_stream()
+    for _ in range(3):
+        sort_entries(src.data_ptr(), dst.data_ptr(), n, key_bits, stream.cuda_stream)
+    reps = 10
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        sort_entries(src.data_ptr(), dst.data_ptr(), n, key_bits, stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    passes = (key_bits + 7) // 8
+    algo = n * 8 * 2 * passes
+    k = (dst >> 32)
+    ok = bool((k[1:] >= k[:-1]).all().item()) and int(dst.sum().item()) == int(src.sum().item())
+    peak = _measured_peak_gbs()
+    gbs = algo / (ms * 1e-3) / 1e9
+    return {"entries": n, "key_bits": key_bits, "passes": passes, "ms": ms, "algorithmic_gb": algo / 1e9,
+            "achieved_gbs": gbs, "peak_gbs": peak, "frac": gbs / peak if peak else None, "sorted": ok,
+            "entries_per_s": n / (ms * 1e-3)}
 
 
 def run_refstore(args):
@@ -598,6 +650,7 @@ def main():
         batched = run_batched(args) if args.batched_batches > 0 and world == 1 else None
         configs = run_config_legs(args) if args.config_legs and world == 1 else None
         refstore = run_refstore(args) if not args.no_refstore and world == 1 else None
+        sort = run_sort(args) if args.sort_entries > 0 and world == 1 else None
         line = {"metric": METRIC, "value": value, "unit": "reads/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
@@ -615,6 +668,7 @@ def main():
                 "batched": batched,
                 "configs": configs,
                 "refstore": refstore,
+                "sort": sort,
                 "clocks": res["clocks"],
                 "stage_ms": [round(x, 3) for x in res["stage_ms"]],
                 "baq_reads": res["stats"]["baq_reads"],

@@ -99,57 +99,123 @@ void scan_rec(const u32 *in, u32 *out, u64 n, u32 *tmp, cudaStream_t s) {
 }
 
 // ---- radix sort ----
+// A tile of RS_TILE keys per block; warp w of the block takes the tile's w-th run of RS_WARP_KEYS consecutive
+// keys, 32 per round, so tile order is (warp, round, lane). The scatter pass ranks each key among the equal
+// digits before it in tile order (warp-private counters, no block barrier per round), reorders the tile by
+// digit in shared memory, and writes each digit's run with consecutive threads on consecutive addresses.
 constexpr int RS_THREADS = 256;
 constexpr int RS_WARPS = RS_THREADS / 32;
-constexpr int RS_ROUNDS = 8;
+constexpr int RS_ROUNDS = 16;
+constexpr int RS_WARP_KEYS = 32 * RS_ROUNDS;
 constexpr int RS_TILE = RS_THREADS * RS_ROUNDS;
 
 __device__ __forceinline__ u32 digit_of(u64 v, int shift) { return u32(v >> (32 + shift)) & 0xFFu; }
 
+// The lanes of the warp holding a key with digit d (the caller's own lane included), from one ballot per digit
+// bit; lanes without a key form their own group. Votes run on the integer pipe, where a match instruction
+// would queue on the warp-divergence unit (measured: that unit 84-89% busy, the sort issue-bound on it).
+__device__ __forceinline__ u32 digit_peers(u32 d, bool valid) {
+    const u32 vm = __ballot_sync(FULL, valid);
+    u32 peers = valid ? vm : ~vm;
+#pragma unroll
+    for (int b = 0; b < 8; b++) {
+        const bool bit = (d >> b) & 1u;
+        const u32 m = __ballot_sync(FULL, bit);
+        peers &= bit ? m : ~m;
+    }
+    return peers;
+}
+
 __global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const u64 *in, u64 n, int shift, u32 *hist, u32 nblocks) {
-    __shared__ u32 h[256];
-    h[threadIdx.x] = 0;
+    __shared__ u32 h[RS_WARPS][256];  // per warp: only its own lanes update it
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int j = threadIdx.x; j < RS_WARPS * 256; j += RS_THREADS) (&h[0][0])[j] = 0;
     __syncthreads();
-    const u64 base = u64(blockIdx.x) * RS_TILE;
-    for (int rnd = 0; rnd < RS_ROUNDS; rnd++) {
-        const u64 i = base + u64(rnd) * RS_THREADS + threadIdx.x;
-        if (i < n) atomicAdd(&h[digit_of(in[i], shift)], 1u);
+    const u64 wbase = u64(blockIdx.x) * RS_TILE + u64(warp) * RS_WARP_KEYS;
+    u64 v[RS_ROUNDS];
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; r++) {
+        const u64 i = wbase + u64(r) * 32 + lane;
+        v[r] = i < n ? in[i] : 0;
+    }
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; r++) {
+        const bool valid = wbase + u64(r) * 32 + lane < n;
+        const u32 d = digit_of(v[r], shift);
+        const u32 peers = digit_peers(d, valid);
+        // one update per distinct digit (distinct addresses within the instruction)
+        if (valid && int(__ffs(peers)) - 1 == lane) h[warp][d] += u32(__popc(peers));
+        __syncwarp();  // the next round's updater of a digit may be another lane
     }
     __syncthreads();
-    hist[u64(threadIdx.x) * nblocks + blockIdx.x] = h[threadIdx.x];
+    u32 t = 0;
+#pragma unroll
+    for (int w = 0; w < RS_WARPS; w++) t += h[w][threadIdx.x];
+    hist[u64(threadIdx.x) * nblocks + blockIdx.x] = t;
 }
 
 __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const u64 *in, u64 n, int shift, const u32 *offs,
                                                            u32 nblocks, u64 *out) {
-    __shared__ u32 running[256];
-    __shared__ u32 wc[RS_WARPS][256];
+    __shared__ u64 buf[RS_TILE];            // the tile ordered by digit
+    __shared__ u32 wcnt[RS_WARPS][256];     // per warp: digit counts, then the warp's first slot per digit
+    __shared__ u32 tstart[256];             // first slot of each digit in the ordered tile
+    __shared__ u32 gbase[256];              // global position of this tile's first key of each digit
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    running[threadIdx.x] = offs[u64(threadIdx.x) * nblocks + blockIdx.x];
-    const u64 base = u64(blockIdx.x) * RS_TILE;
     const u32 lt = (1u << lane) - 1;
-    for (int rnd = 0; rnd < RS_ROUNDS; rnd++) {
-        for (int j = threadIdx.x; j < RS_WARPS * 256; j += RS_THREADS) (&wc[0][0])[j] = 0;
-        __syncthreads();
-        const u64 i = base + u64(rnd) * RS_THREADS + threadIdx.x;
-        const bool valid = i < n;
-        const u64 v = valid ? in[i] : 0;
-        const u32 d = valid ? digit_of(v, shift) : 256u;
-        const u32 peers = __match_any_sync(FULL, d);
-        const u32 rank = __popc(peers & lt);
-        if (valid && rank == 0) wc[warp][d] = __popc(peers);
-        __syncthreads();
-        if (valid) {
-            u32 pre = 0;
-            for (int w2 = 0; w2 < warp; w2++) pre += wc[w2][d];
-            out[running[d] + pre + rank] = v;
+    for (int j = threadIdx.x; j < RS_WARPS * 256; j += RS_THREADS) (&wcnt[0][0])[j] = 0;
+    gbase[threadIdx.x] = offs[u64(threadIdx.x) * nblocks + blockIdx.x];
+    __syncthreads();
+    const u64 tile0 = u64(blockIdx.x) * RS_TILE;
+    const u64 wbase = tile0 + u64(warp) * RS_WARP_KEYS;
+    u64 v[RS_ROUNDS];
+    u32 rank[RS_ROUNDS / 2];  // per key: the warp's earlier keys with the same digit (< 512), two per word
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; r++) {
+        const u64 i = wbase + u64(r) * 32 + lane;
+        v[r] = i < n ? in[i] : 0;
+    }
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; r++) {
+        const bool valid = wbase + u64(r) * 32 + lane < n;
+        const u32 d = digit_of(v[r], shift);
+        const u32 peers = digit_peers(d, valid);
+        const u32 before = valid ? wcnt[warp][d] : 0u;  // the digit's peers read one word together
+        const u32 rk = before + u32(__popc(peers & lt));
+        if (r & 1) rank[r >> 1] |= rk << 16;
+        else rank[r >> 1] = rk;
+        __syncwarp();
+        if (valid && int(__ffs(peers)) - 1 == lane) wcnt[warp][d] = before + u32(__popc(peers));
+        __syncwarp();
+    }
+    __syncthreads();
+    {
+        // thread d: the digit's count over the warps (warp-major within the digit), then its place in the tile
+        const u32 d = threadIdx.x;
+        u32 run = 0;
+#pragma unroll
+        for (int w = 0; w < RS_WARPS; w++) {
+            const u32 c = wcnt[w][d];
+            wcnt[w][d] = run;
+            run += c;
         }
-        __syncthreads();
-        {
-            u32 tot = 0;
-            for (int w2 = 0; w2 < RS_WARPS; w2++) tot += wc[w2][threadIdx.x];
-            running[threadIdx.x] += tot;
-        }
-        __syncthreads();
+        u32 total;
+        const u32 start = block_exclusive_scan(run, &total);
+        tstart[d] = start;
+#pragma unroll
+        for (int w = 0; w < RS_WARPS; w++) wcnt[w][d] += start;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; r++) {
+        const u64 i = wbase + u64(r) * 32 + lane;
+        if (i < n) buf[wcnt[warp][digit_of(v[r], shift)] + ((rank[r >> 1] >> ((r & 1) * 16)) & 0xFFFFu)] = v[r];
+    }
+    __syncthreads();
+    const u32 tile_n = u32(n - tile0 < u64(RS_TILE) ? n - tile0 : u64(RS_TILE));
+    for (u32 p = threadIdx.x; p < tile_n; p += RS_THREADS) {
+        const u64 key = buf[p];
+        const u32 d = digit_of(key, shift);
+        out[gbase[d] + (p - tstart[d])] = key;
     }
 }
 

@@ -123,6 +123,7 @@ def sort_entries(d_in: int, d_out: int, n: int, key_bits: int, stream: int = 0) 
         raise EngineError(f"fp_sort_entries: {STATUS_NAMES.get(rc, rc)}")
 
 
+
 class Engine:
     """One GB300 BQSR engine (fp_engine handle)."""
 

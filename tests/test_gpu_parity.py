@@ -151,6 +151,30 @@ def test_batch_size_independent(native):
     assert_tables_equal(t1, t2)
 
 
+def test_growing_and_shrinking_batches_with_overlapped_folds(native):
+    """Each batch's sort + fold runs on the fold stream while the next batch starts: batches whose entry
+    buffers must grow (the previous fold is waited for first), shrink again, and a reset in the middle of a
+    stream (the pending fold is joined) give the oracle's tables."""
+    from firepony_gb300.engine import Engine
+    p, ref, batches = make_dataset("precision_20M_151bp_pe", 24000, 24000, 600_000)
+    whole = batches[0]
+    cuts = [0, 300, 1300, 9300, 23300, 23800, 24000]  # 300, 1000, 8000, 14000, 500, 200 reads
+    parts = [whole.subset(np.arange(a, b)) for a, b in zip(cuts, cuts[1:])]
+    e = Engine(num_read_groups=p.num_read_groups)
+    try:
+        e.load_reference(ref)
+        for b in parts[:4]:
+            e.submit(b)
+        e.reset()  # drops those batches; their folds are joined first
+        for b in parts:
+            e.submit(b)
+        got = e.finalize()
+    finally:
+        e.close()
+    want, _, _ = run_oracle(ref, [whole], p.num_read_groups)
+    assert_tables_equal(got, want)
+
+
 def test_report_identical(native, tmp_path):
     from firepony_gb300.engine import Engine, write_report
     p, ref, batches = make_dataset("precision_20M_151bp_pe", 4000, 2000, 300_000)

@@ -10,7 +10,8 @@ def reference_sort(a, key_bits):
     return a[np.argsort(key, kind="stable")]
 
 
-@pytest.mark.parametrize("n,key_bits", [(1, 8), (1000, 8), (70_001, 20), (1 << 20, 28), (3_000_017, 24)])
+@pytest.mark.parametrize("n,key_bits", [(1, 8), (1000, 8), (4097, 12), (70_001, 20), (1 << 20, 28), (3_000_017, 24),
+                                        (2_000_003, 32)])
 def test_sort_entries_stable(native, n, key_bits):
     import torch
     from firepony_gb300.engine import sort_entries
@@ -26,3 +27,23 @@ def test_sort_entries_stable(native, n, key_bits):
     np.testing.assert_array_equal(got, reference_sort(a, key_bits))
     # the input is left untouched
     np.testing.assert_array_equal(d_in.cpu().numpy().view(np.uint64), a)
+
+
+def test_sort_entries_skewed_digits(native):
+    """Covariate keys are dense and skewed: long runs share their high digits and a few keys take most
+    entries. Runs of one digit across whole warps and tiles, and tiles of a single key, keep the order."""
+    import torch
+    from firepony_gb300.engine import sort_entries
+    rng = np.random.default_rng(11)
+    n = 1_500_000
+    hot = rng.integers(0, 40, n // 2, dtype=np.uint64)            # a few hot keys
+    cold = rng.integers(0, 1 << 21, n - n // 2, dtype=np.uint64)  # spread over 21 bits
+    keys = np.concatenate([np.sort(hot)[: n // 4], hot[n // 4:], cold])
+    keys[:300_000] = 7                                             # one key over many whole tiles
+    payload = np.arange(n, dtype=np.uint64)
+    a = (keys << np.uint64(32)) | payload
+    d_in = torch.from_numpy(a.view(np.int64).copy()).cuda()
+    d_out = torch.empty_like(d_in)
+    sort_entries(d_in.data_ptr(), d_out.data_ptr(), n, 29)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(d_out.cpu().numpy().view(np.uint64), reference_sort(a, 29))
