@@ -11,6 +11,16 @@
 // The forward row sums only set the row scaling, a common factor that cancels in every posterior ratio, and
 // the chains along a row (the D recurrences) run on the group's first lane in slot order.
 //
+// Cells far from the alignment decay by many orders of magnitude across a wide band. Instead of giving up on
+// a read with such a cell, a computed cell value below FLUSH is replaced by zero. Every operand of the
+// recurrences is then zero or at least FLUSH; the smallest factors are a mismatch emission (1.7e-10), the
+// gap-open transition (>= 7.5e-5) and 0.1, so every product and sum of kept values stays at or above
+// FLUSH * 2^-34 > 2^-126 and the relative error analysis above holds for them. Each flushed value carries an
+// absolute error below FLUSH, whose effect on the posterior terms is bounded separately (backward values are
+// at most 1 and forward values at most the row sum in the scaled units; see the error terms below) and added
+// to the decision margins as an absolute error. Posterior products of kept values may still underflow: each
+// adds at most 2^-150.
+//
 // Slot s of row i holds cell k = s + x(i), x(i) = max(i - bw, 0); rows are exchanged through per-group shared
 // buffers indexed by slot + 1 with zero sentinels. A group whose read has a band wider than WC takes no read
 // (the thread-per-read FP64 kernel computes those). Per group scratch (global): rows 0..max_q+1 of 2*WC+1
@@ -29,7 +39,15 @@ constexpr int WD_THREADS = 128;
 constexpr float FWD_SCALE = 18446744073709551616.0f;          // 2^64 (forward rows sum to 2^64)
 constexpr float BWD_INIT = 79228162514264337593543950336.0f;  // 2^96 = 2^64 (sLast) x 2^32 (backward factor)
 
-__device__ __forceinline__ bool tiny_pos(float v) { return (__float_as_uint(v) - 1u) < (0x1AF1C901u - 1u); }
+constexpr float FLUSH = 3.3087224502121107e-24f;  // 2^-78
+
+// v < FLUSH -> 0, counting the values that were not zero already
+__device__ __forceinline__ void flush(float &v, float &c) {
+    if (v < FLUSH) {
+        c += v > 0.0f ? 1.0f : 0.0f;
+        v = 0.0f;
+    }
+}
 
 // sums / maxima over the G lanes of a group (every lane gets the result)
 template <int G> __device__ __forceinline__ float gsum(float v) {
@@ -149,7 +167,9 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
         const float m3 = float((1 - 0.1) * (1 - dsM)), m4 = float(0.1 * (1 - dsM));
         const float m6 = float(1 - 0.1), m8 = float(0.1);
         const float EIm1 = EI * m1, EIm4 = EI * m4;
-        bool under = false;
+        // forward flush errors in units of FLUSH, carried to row qL's scale: K = (K + before-scaling flushes)
+        // * inv + after-scaling flushes, row by row (each lane its own flushes; the terms add up)
+        float kf = 0.0f;
 
         // ---- forward, row 1: slot s = cell k, band [1, min(refLen, bw + 1)] ----
         float fM[NS], fI[NS], fD[NS];
@@ -175,11 +195,14 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
                 const int s = l + j * G;
                 fM[j] *= inv1;
                 fI[j] *= inv1;
+                float c = 0.0f;
+                flush(fM[j], c);
+                flush(fI[j], c);
+                if (act) kf += c;
                 if (act) {
                     FROW(1)[s] = fM[j];
                     FROW(1)[WC + s] = fI[j];
                 }
-                if (tiny_pos(fM[j])) under = true;
                 PM[s + 1] = fM[j];
                 PI[s + 1] = fI[j];
                 PD[s + 1] = 0.0f;
@@ -200,6 +223,7 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
             const int shi = int(__reduce_max_sync(FULL, u32(act ? (end - x < WC - 1 ? end - x : WC - 1) : 0)));
             // M and I of every slot from the previous row; m2 * M feeds the D chain of the next slot
             float mI[NS];
+            float cpre = 0.0f;  // this lane's flushes of the row before its scaling
 #pragma unroll
             for (int j = 0; j < NS; j++) {
                 const int s = l + j * G, k = s + x;
@@ -212,6 +236,8 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
                     const float e = EMI(REF(k - 1), qy, qq);
                     m = e * ((m0 * oM + m3 * oI) + m6 * oD);
                     ii = EI * (m1 * nM1 + m4 * nI1);
+                    flush(m, cpre);
+                    flush(ii, cpre);
                 }
                 fM[j] = m;
                 fI[j] = ii;
@@ -225,6 +251,8 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
                 float d = 0.0f;  // (zero at and below the lowest band slot)
                 for (int s = slo; s <= shi; s++) {
                     d = (s == 0 ? 0.0f : X0[s]) + m8 * d;
+                    // (a chain value past the band is discarded; its flush only adds to the bound)
+                    flush(d, cpre);
                     X1[s] = d;
                 }
             }
@@ -241,26 +269,31 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
             const float inv = act ? FWD_SCALE / sum : 0.0f;
             if (act && l == 0) FROW(i)[2 * WC] = sum;
             __syncwarp();  // every lane has read the previous row before it is replaced
+            float cpost = 0.0f;
 #pragma unroll
             for (int j = 0; j < NS; j++) {
                 const int s = l + j * G;
                 fM[j] *= inv;
                 fI[j] *= inv;
                 fD[j] *= inv;
+                flush(fM[j], cpost);
+                flush(fI[j], cpost);
+                flush(fD[j], cpost);
                 PM[s + 1] = fM[j];
                 PI[s + 1] = fI[j];
                 PD[s + 1] = fD[j];
                 if (act) {
                     FROW(i)[s] = fM[j];
                     FROW(i)[WC + s] = fI[j];
-                    if (tiny_pos(fM[j])) under = true;
                 }
             }
+            if (act) kf = (kf + cpre) * inv + cpost;
             __syncwarp();
         }
 
         // ---- s[qL+1] and the backward start (device/baq.cu:520-545), as k_baq_tpr<float> ----
         float bMv[NS], bIv[NS];
+        float ef = 0.0f;  // forward flush error bound relative to the posterior total
         {
             const int x = qL - bw > 0 ? qL - bw : 0;
             bool cell[NS];
@@ -274,6 +307,12 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
                 part += cell[j] ? lm * sM + lI * sI : 0.0f;
             }
             const float sLast = gsum<G>(part);
+            // forward flushes, relative to the posterior total: an error e (row j's scaled units) reaches every
+            // posterior sum through backward values <= 1 (reference units), i.e. at most e * prod(inv of the
+            // rows after j) / sLast of the total; 1.01 covers the rounding of the bound itself
+            const float kf_all = gsum<G>(kf);
+            ef = kf_all > 0.0f ? 1.01f * FLUSH * kf_all / sLast : 0.0f;
+            if (!(ef < 1.0f)) ef = __int_as_float(0x7f800000);
             const float sQ = qL >= 1 ? FROW(qL)[2 * WC] : 1.0f;
             // sM / s(qL) / sLast in reference units, times 2^32: sQ carries 2^64 unless qL == 1, sLast 2^64
             const float v = ((sM / sQ) * (qL >= 2 ? FWD_SCALE : 1.0f) / sLast) * BWD_INIT;
@@ -294,11 +333,16 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
         const float rel = 2.0f * (eps_z + 2.0f * WC * u) + u;
         const float rel_state = 2.0f * eps_z + 2.0f * u;
         const float dt = 4.343f * rel / (1.0f - rel) + 1e-4f;
+        // backward flushes, relative to the posterior total, over the rows done so far (qL down to i): an error
+        // e in a backward value of row i' reaches every posterior sum through that cell's forward value, at
+        // most the forward row sum 2^64, i.e. at most e * 2^64 / (row i' posterior sum) of the total
+        float eb = 0.0f;
 
         // ---- backward fused with MAP, rows qL..1 of every group (t steps back from its own last row) ----
         for (int t = 0; t < Qmax; t++) {
             const int i = qL - t;
             const bool act = i >= 1;
+            float rowflush = 0.0f;  // this lane's backward flush errors of row i (its scaled units, in FLUSH)
             const int beg = 1 > i - bw ? 1 : i - bw;
             const int end = refLen < i + bw ? refLen : i + bw;
             const int x = i - bw > 0 ? i - bw : 0;
@@ -309,6 +353,7 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
                 const bool y = i > 1;
                 const u8 qy1 = act ? QRY(i) : 0, qq1 = act ? QUL(i) : 0;
                 float a1[NS];
+                float cbpre = 0.0f;  // this lane's flushes of the row before its scaling
 #pragma unroll
                 for (int j = 0; j < NS; j++) {
                     const int s = l + j * G, k = s + x;
@@ -330,12 +375,14 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
                     X1[shi + 1] = 0.0f;
                     for (int s = shi; s >= slo; s--) {
                         d = y ? X0[s] + m8 * d : 0.0f;
+                        flush(d, cbpre);
                         X1[s] = d;
                     }
                 }
                 __syncwarp();
                 // 1 / s(i) in reference units: s(i) carries 2^64 for rows after the first
                 const float yy = act ? (i == 1 ? 1.0f : FWD_SCALE) / FROW(i)[2 * WC] : 0.0f;
+                float cbpost = 0.0f;
 #pragma unroll
                 for (int j = 0; j < NS; j++) {
                     const int s = l + j * G, k = s + x;
@@ -343,9 +390,10 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
                     const float bm = inb ? a1[j] + m2 * X1[s + 1] : 0.0f;
                     bMv[j] = bm * yy;
                     bIv[j] = bIv[j] * yy;
-                    // (cells of column refLen may decay through the subnormal range unflagged, as in k_baq_tpr)
-                    if (act && k <= refLen - 1 && tiny_pos(bMv[j])) under = true;
+                    flush(bMv[j], cbpost);
+                    flush(bIv[j], cbpost);
                 }
+                rowflush = act ? cbpre * yy + cbpost : 0.0f;
                 __syncwarp();
 #pragma unroll
                 for (int j = 0; j < NS; j++) {
@@ -355,6 +403,7 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
                 }
             }
             // ---- MAP for row i (device/baq.cu:619-681) with the certified decisions of k_baq_tpr<float> ----
+            // (the flush errors of this row's backward values join the bound once the row's sum is known)
             // posterior terms of the in-band cells; the first maximum in (k, M before I) order: non-negative
             // floats order like their bit patterns, ties keep the smaller index
             float z[2 * NS];
@@ -394,7 +443,15 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
             }
             const float excl = gsum<G>(ex), second = gmax<G>(sec);
             const bool valid = sum > 0.0f && sum <= 3.0e38f && bbits != 0;
-            const float thr = mx * (1.0f - rel_state);
+            // absolute error of the posterior terms, relative to the row's exact total (the computed sum is
+            // within a factor 2 of it): forward flushes, backward flushes of rows qL..i, and underflowed products
+            const float rf = gsum<G>(rowflush);
+            if (valid && rf > 0.0f) eb += 2.02f * FLUSH * rf * FWD_SCALE / sum;
+            // underflowed products: at most 2^-150 each, 2 WC terms (2^-148 per term, in the row's units)
+            const float ez = 2.0f * WC * __int_as_float(4);
+            float abs_err = (ef + eb) * sum + ez;  // in the row's units
+            if (!(abs_err < 3.0e38f)) abs_err = __int_as_float(0x7f800000);
+            const float thr = mx * (1.0f - rel_state) - 2.0f * abs_err;
             // an undecided state records its rival when there is exactly one
             u32 rivals = 0, alt = 0xFFFFFFFFu;
             if (gany<G>(act && valid && second >= thr)) {
@@ -432,7 +489,21 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
                     }
                     const float ratio = excl / sum;
                     const float tq = ratio > 0.f ? -4.343f * logf(ratio) + 0.499f : __int_as_float(0x7f800000);
-                    const float lo = tq - dt, hi = tq + dt;
+                    float lo = tq - dt, hi = tq + dt;
+                    // the absolute error moves the other terms' sum by at most abs_err: t by at most
+                    // 4.343 * ln(1 + abs_err / excl); when that is large, only the lower bound of t is kept
+                    const float extra = abs_err > 0.0f ? (excl > 0.0f ? abs_err / excl : __int_as_float(0x7f800000)) : 0.0f;
+                    if (extra > 0.0f) {
+                        if (extra < 0.25f) {
+                            const float dta = 4.343f * extra / (1.0f - extra);
+                            lo -= dta;
+                            hi += dta;
+                        } else {
+                            const float rhi = (excl * (1.0f + rel) + abs_err) / (sum * (1.0f - rel));
+                            lo = -4.343f * logf(rhi) + 0.499f - 1e-4f;
+                            hi = __int_as_float(0x7f800000);
+                        }
+                    }
                     qv = capped_q(tq);
                     const int flo = capped_q(lo), fhi = capped_q(hi);
                     if (qo <= 99) {
@@ -446,9 +517,6 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
                 w.baq_amb[qi] = amb;
             }
         }
-        // a read with a value that could leave the normal range is undecided throughout
-        if (gany<G>(under) && has)
-            for (int row = l; row < qL; row += G) w.baq_amb[qual0 + u32(row)] = 7;
         __syncwarp();
     }
 }

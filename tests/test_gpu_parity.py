@@ -258,6 +258,37 @@ def test_replay_all_wide_bands(native):
     assert_tables_equal(te, to)
 
 
+def test_wide_band_fp32_decisions_match_fp64(native):
+    """The certified FP32 kernel for bands 16..31 flushes far cells to zero and widens its decision margins by
+    the bound on the error that introduces. Over an uneven-batch workload, every BQ tag of the FP32 path
+    (decided in FP32, or replayed in FP64 where undecided) equals the plain FP64 path's, batch by batch, and
+    most wide-band reads are decided without a replay."""
+    from firepony_gb300.engine import Engine
+    p, ref, batches = make_dataset("batched_uneven", 48000, 6000, 800_000)
+    e32 = Engine(num_read_groups=p.num_read_groups, baq_mode="fp32")
+    e64 = Engine(num_read_groups=p.num_read_groups, baq_mode="fp64")
+    try:
+        for e in (e32, e64):
+            e.load_reference(ref)
+        for b in batches:
+            e32.submit(b)
+            d32 = e32.debug_last_batch(b)
+            e64.submit(b)
+            d64 = e64.debug_last_batch(b)
+            np.testing.assert_array_equal(d32["read_status"], d64["read_status"])
+            np.testing.assert_array_equal(d32["baq_tag"], d64["baq_tag"], err_msg="BQ tags")
+        t32, t64 = e32.finalize(), e64.finalize()
+        s32 = e32.stats()
+    finally:
+        e32.close()
+        e64.close()
+    assert_tables_equal(t32, t64)
+    wide = s32["baq_reads_by_band"][2]
+    assert wide > 1000
+    # escalations of the wider classes (1 and 2 together) stay well below the wide-band read count
+    assert s32["baq_escalated_by_band"][1] < 0.5 * wide, (s32["baq_escalated_by_band"], wide)
+
+
 def test_replay_all_edge_cases(native):
     from firepony_gb300.abi import FP_FLAG_REPLAY_ALL
     from tests.edge_cases import edge_case_dataset
