@@ -64,6 +64,21 @@ __device__ __forceinline__ bool tiny_positive(float v) {
 }
 __device__ __forceinline__ bool tiny_positive(double) { return false; }
 
+// Band class 1 (FP32, 31 slots) replaces the read-level guard above by flushing: a computed value below
+// FLUSH_T becomes zero, so every operand is zero or at least 2^-78 and every kept product and sum stays at
+// or above 2^-112 (normal), and each flush's absolute error (below 2^-78 in the units of its row) is bounded
+// and added to the decision margins. The bound: a forward error e in row j reaches the posterior terms
+// through backward values of at most 1 (reference units), i.e. at most e * prod(inv of the rows after j) /
+// sLast of the posterior total; a backward error e in row i through forward values of at most the row sum
+// 2^64, i.e. at most e * 2^64 / (row i's posterior sum); an underflowed posterior product adds at most 2^-150.
+constexpr float FLUSH_T = 3.3087224502121107e-24f;  // 2^-78
+template <typename T> __device__ __forceinline__ void flush_t(T &v, float &c) {
+    if (v < T(FLUSH_T)) {
+        c += v > T(0) ? 1.0f : 0.0f;
+        v = T(0);
+    }
+}
+
 template <typename T>
 __device__ __forceinline__ T emission(const T *em_tab, const T *mis_tab, u8 ref, u8 rd, u8 q) {
     if (ref == IUPAC_N || rd == IUPAC_N) return T(1);
@@ -88,6 +103,7 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                                                          const u32 *count, u32 *work_ctr, T *scratch, u32 max_q,
                                                          u32 rpw) {
     using A = Ar<T, EXACT>;
+    constexpr bool FL = !EXACT && W == 31;  // flush-and-bound instead of the read-level guard
     __shared__ T s_em[256], s_mis[256];
     for (int q = threadIdx.x; q < 256; q += blockDim.x) {
         const double p = ct_qual2prob[q < MIN_BASE_QUAL ? MIN_BASE_QUAL : q];
@@ -146,6 +162,7 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
         const T m3 = T((1 - 0.1) * (1 - dsM)), m4 = T(0.1 * (1 - dsM));
         const T m6 = T(1 - 0.1), m8 = T(0.1);
         bool under = false;
+        float kf = 0.0f;  // FL: forward flush errors (units of FLUSH_T) carried to row qL's scale
         // interior rows (every slot in the band, no cell at the reference end) take the branch-free path
         const bool full = 2 * bw + 1 == W;
         const T EIm1 = A::mul(EI, m1), EIm4 = A::mul(EI, m4);
@@ -182,9 +199,13 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                     M[s] = M[s] * inv1;
                     I[s] = I[s] * inv1;
                 }
+                if constexpr (FL) {
+                    flush_t(M[s], kf);
+                    flush_t(I[s], kf);
+                }
                 FS(1, s, 0) = M[s];
                 FS(1, s, 1) = I[s];
-                if (tiny_positive(M[s])) under = true;
+                if (!FL && tiny_positive(M[s])) under = true;
             }
         }
         // ---- forward, rows 2..qL ----
@@ -202,6 +223,7 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
             const int end = refLen < i + bw ? refLen : i + bw;
             const int x = i - bw > 0 ? i - bw : 0;  // slot s holds cell k = s + x
             T sum = T(0);
+            float cpre = 0.0f;  // FL: flushes of the row before its scaling
             if (full && i > bw && i + bw < refLen) {
 #pragma unroll
                 for (int s = 0; s < W - 1; s++) rw[s] = rw[s + 1];
@@ -214,9 +236,14 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                     const T oM = M[s], oI = I[s], oD = D[s];
                     const T nM1 = s + 1 < W ? M[s + 1] : T(0), nI1 = s + 1 < W ? I[s + 1] : T(0);
                     const T e = cell_emission<T>(rw[s], qyi, eq, ex);
-                    const T m = A::mul(e, A::add(A::add(A::mul(m0, oM), A::mul(m3, oI)), A::mul(m6, oD)));
-                    const T ii = A::mul(EI, A::add(A::mul(m1, nM1), A::mul(m4, nI1)));
-                    const T d = A::add(A::mul(m2, mprev), A::mul(m8, dprev));
+                    T m = A::mul(e, A::add(A::add(A::mul(m0, oM), A::mul(m3, oI)), A::mul(m6, oD)));
+                    T ii = A::mul(EI, A::add(A::mul(m1, nM1), A::mul(m4, nI1)));
+                    if constexpr (FL) {
+                        flush_t(m, cpre);
+                        flush_t(ii, cpre);
+                    }
+                    T d = A::add(A::mul(m2, mprev), A::mul(m8, dprev));
+                    if constexpr (FL) flush_t(d, cpre);
                     sum = A::add(sum, A::add(A::add(m, ii), d));
                     M[s] = m; I[s] = ii; D[s] = d;
                     mprev = m; dprev = d;
@@ -239,7 +266,12 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                         const T e = emission<T>(s_em, s_mis, rw[s], qyi, qq);
                         m = A::mul(e, A::add(A::add(A::mul(m0, oM), A::mul(m3, oI)), A::mul(m6, oD)));
                         ii = A::mul(EI, A::add(A::mul(m1, nM1), A::mul(m4, nI1)));
+                        if constexpr (FL) {
+                            flush_t(m, cpre);
+                            flush_t(ii, cpre);
+                        }
                         d = A::add(A::mul(m2, mprev), A::mul(m8, dprev));
+                        if constexpr (FL) flush_t(d, cpre);
                         sum = A::add(sum, A::add(A::add(m, ii), d));
                     }
                     M[s] = m; I[s] = ii; D[s] = d;
@@ -258,6 +290,10 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                                 pD = s >= 1 ? D[s - 1] : T(0);
                         m = A::mul(e, A::add(A::add(A::mul(m0, pM), A::mul(m3, pI)), A::mul(m6, pD)));
                         ii = A::mul(EI, A::add(A::mul(m1, M[s]), A::mul(m4, I[s])));
+                        if constexpr (FL) {
+                            flush_t(m, cpre);
+                            flush_t(ii, cpre);
+                        }
                     }
                     M[s] = m; I[s] = ii;
                 }
@@ -269,6 +305,7 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                     T d = T(0);
                     if (inb) {
                         d = A::add(A::mul(m2, mprev), A::mul(m8, dprev));
+                        if constexpr (FL) flush_t(d, cpre);
                         sum = A::add(sum, A::add(A::add(M[s], I[s]), d));
                     }
                     D[s] = d;
@@ -277,15 +314,22 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
             }
             SC(i) = sum;
             const T inv = A::div(EXACT ? T(1) : T(FWD_SCALE), sum);
+            float cpost = 0.0f;
 #pragma unroll
             for (int s = 0; s < W; s++) {
                 M[s] = A::mul(M[s], inv);
                 I[s] = A::mul(I[s], inv);
                 D[s] = A::mul(D[s], inv);
+                if constexpr (FL) {
+                    flush_t(M[s], cpost);
+                    flush_t(I[s], cpost);
+                    flush_t(D[s], cpost);
+                }
                 FS(i, s, 0) = M[s];
                 FS(i, s, 1) = I[s];
-                if (tiny_positive(M[s])) under = true;
+                if (!FL && tiny_positive(M[s])) under = true;
             }
+            if constexpr (FL) kf = (kf + cpre) * float(inv) + cpost;
         }
         // s[qL+1]: band cells of row qL (slots 0..2bw with k in [1, refLen])
         T sLast = T(0);
@@ -298,6 +342,13 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
             }
         }
         const T sQ = SC(qL);
+        // FL: forward flush errors relative to the posterior total (1.01 covers the rounding of the bound)
+        float ef = 0.0f;
+        if constexpr (FL) {
+            ef = kf > 0.0f ? 1.01f * FLUSH_T * kf / float(sLast) : 0.0f;
+            if (!(ef < 1.0f)) ef = __int_as_float(0x7f800000);
+        }
+        float eb = 0.0f;  // FL: backward flush errors of the rows done so far, relative to the posterior total
 
         // ---- backward fused with MAP ----
         // slot s of row i holds cell k = s + x(i); the reference symbol it needs is REF(k)
@@ -365,7 +416,9 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                 fM[s] = FS(i, s, 0);
                 fI[s] = FS(i, s, 1);
             }
+            float rowflush = 0.0f;  // FL: this row's backward flush errors (its scaled units, in FLUSH_T)
             if (i < qL) {
+                float cbpre = 0.0f;
                 const u8 qyi1 = nq, qq1 = nqq, ref0 = nref;
                 if (i > 1) {
                     nq = QRY(i - 1);
@@ -393,7 +446,8 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                         const T e = A::mul(cell_emission<T>(rw[s], qyi1, eq, ex), bMv[s]);
                         const T bm = A::add(A::add(A::mul(e, m0), A::mul(EIm1, bi1)), A::mul(m2, dnext));
                         const T bi = A::add(A::mul(e, m3), A::mul(EIm4, bi1));
-                        const T bd = A::mul(A::add(A::mul(e, m6), A::mul(m8, dnext)), y);
+                        T bd = A::mul(A::add(A::mul(e, m6), A::mul(m8, dnext)), y);
+                        if constexpr (FL) flush_t(bd, cbpre);
                         bMv[s] = bm; bIv[s] = bi; bDv[s] = bd;
                         dnext = bd;
                     }
@@ -415,6 +469,7 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                         bm = A::add(A::add(A::mul(e, m0), A::mul(EIm1, bi1)), A::mul(m2, dnext));
                         bi = A::add(A::mul(e, m3), A::mul(EIm4, bi1));
                         bd = A::mul(A::add(A::mul(e, m6), A::mul(m8, dnext)), y);
+                        if constexpr (FL) flush_t(bd, cbpre);
                     }
                     bMv[s] = bm; bIv[s] = bi; bDv[s] = bd;
                     dnext = bd;
@@ -427,13 +482,19 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                 // own tiny value) may decay through the subnormal range: their absolute error (< 2^-149 per
                 // operation) is below 1e-23 of any cell they feed and is not flagged
                 const int last_ok = refLen - 1 - x;
+                float cbpost = 0.0f;
 #pragma unroll
                 for (int s = 0; s < W; s++) {
                     bMv[s] = A::mul(bMv[s], yy);
                     bIv[s] = A::mul(bIv[s], yy);
                     bDv[s] = A::mul(bDv[s], yy);
-                    if (tiny_positive(bMv[s]) && s <= last_ok) under = true;
+                    if constexpr (FL) {
+                        flush_t(bMv[s], cbpost);
+                        flush_t(bIv[s], cbpost);
+                    }
+                    if (!FL && tiny_positive(bMv[s]) && s <= last_ok) under = true;
                 }
+                if constexpr (FL) rowflush = cbpre * float(yy) + cbpost;
             }
             // ---- MAP for row i (device/baq.cu:619-681): first maximum in (k, M before I) order ----
             T sum = T(0), mx = T(0), second = T(0), excl = T(0);
@@ -477,6 +538,14 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
             }
             }
             const u32 qi = qual0 + u32(i - 1);
+            if constexpr (FL) {
+                // this row's backward flushes join the bound before its decisions (a row without a usable sum
+                // leaves every later row undecided)
+                if (rowflush > 0.0f)
+                    eb = (float(sum) > 0.0f && float(sum) <= 3.0e38f)
+                             ? eb + 2.02f * FLUSH_T * rowflush * FWD_SCALE / float(sum)
+                             : __int_as_float(0x7f800000);
+            }
             if (EXACT) {
                 const double p = double(A::div(mx, sum));
                 // -4.343 * log(1 - max) + .499 with no fused operation; (int) saturates like the reference's
@@ -495,7 +564,12 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                     amb = 7;
                 } else {
                     state = u32(max_k);
-                    const float thr = float(mx) * (1.0f - rel_state);
+                    float abs_err = 0.0f;  // FL: absolute error of the posterior terms, in the row's units
+                    if constexpr (FL) {
+                        abs_err = (ef + eb) * float(sum) + 2.0f * W * __int_as_float(4);
+                        if (!(abs_err < 3.0e38f)) abs_err = __int_as_float(0x7f800000);
+                    }
+                    const float thr = float(mx) * (1.0f - rel_state) - 2.0f * abs_err;
                     if (float(second) >= thr) {
                         // undecided state: the rivals are the other cells whose term is within the bound of the
                         // maximum; with exactly one, the capping step can still decide when neither state is the
@@ -523,7 +597,20 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                     }
                     const float ratio = float(excl) / float(sum);
                     const float tq = ratio > 0.f ? -4.343f * logf(ratio) + 0.499f : __int_as_float(0x7f800000);
-                    const float lo = tq - dt, hi = tq + dt;
+                    float lo = tq - dt, hi = tq + dt;
+                    if (FL && abs_err > 0.0f) {
+                        // the other terms' sum moves by at most abs_err: t by 4.343 ln(1 + abs_err / excl)
+                        const float extra = float(excl) > 0.0f ? abs_err / float(excl) : __int_as_float(0x7f800000);
+                        if (extra < 0.25f) {
+                            const float dta = 4.343f * extra / (1.0f - extra);
+                            lo -= dta;
+                            hi += dta;
+                        } else {
+                            const float rhi = (float(excl) * (1.0f + rel) + abs_err) / (float(sum) * (1.0f - rel));
+                            lo = -4.343f * logf(rhi) + 0.499f - 1e-4f;
+                            hi = __int_as_float(0x7f800000);
+                        }
+                    }
                     auto capped = [&](float tt) {
                         int k;
                         if (!(tt == tt)) k = 0;

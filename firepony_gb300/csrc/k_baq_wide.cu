@@ -446,7 +446,8 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
             // absolute error of the posterior terms, relative to the row's exact total (the computed sum is
             // within a factor 2 of it): forward flushes, backward flushes of rows qL..i, and underflowed products
             const float rf = gsum<G>(rowflush);
-            if (valid && rf > 0.0f) eb += 2.02f * FLUSH * rf * FWD_SCALE / sum;
+            // (a row without a usable sum leaves every later row undecided)
+            if (rf > 0.0f) eb = valid ? eb + 2.02f * FLUSH * rf * FWD_SCALE / sum : __int_as_float(0x7f800000);
             // underflowed products: at most 2^-150 each, 2 WC terms (2^-148 per term, in the row's units)
             const float ez = 2.0f * WC * __int_as_float(4);
             float abs_err = (ef + eb) * sum + ez;  // in the row's units
