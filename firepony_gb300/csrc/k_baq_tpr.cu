@@ -162,6 +162,9 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
         const T m3 = T((1 - 0.1) * (1 - dsM)), m4 = T(0.1 * (1 - dsM));
         const T m6 = T(1 - 0.1), m8 = T(0.1);
         bool under = false;
+        // the range arguments take emissions >= 1.7e-10 (base qualities <= 93); a read with a higher quality
+        // (up to 255: 0xFF marks a missing quality string) is left undecided for the exact replay
+        int qmax = QUL(0);
         float kf = 0.0f;  // FL: forward flush errors (units of FLUSH_T) carried to row qL's scale
         // interior rows (every slot in the band, no cell at the reference end) take the branch-free path
         const bool full = 2 * bw + 1 == W;
@@ -214,6 +217,7 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
         u8 nref = REF(W - 1 + (2 - bw > 0 ? 2 - bw : 0) - 1);
         for (int i = 2; i <= qL; i++) {
             const u8 qyi = nq, qq = nqq, top = nref;
+            qmax = qmax > qq ? qmax : qq;
             if (i < qL) {
                 nq = QRY(i);
                 nqq = QUL(i);
@@ -631,7 +635,7 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                 w.baq_amb[qi] = amb;
             }
         }
-        if (!EXACT && under) {
+        if (!EXACT && (under || qmax > 93)) {
             for (int i = 0; i < qL; i++) w.baq_amb[qual0 + i] = 7;
         }
     }

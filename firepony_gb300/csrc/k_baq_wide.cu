@@ -170,6 +170,9 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
         // forward flush errors in units of FLUSH, carried to row qL's scale: K = (K + before-scaling flushes)
         // * inv + after-scaling flushes, row by row (each lane its own flushes; the terms add up)
         float kf = 0.0f;
+        // the range arguments take emissions >= 1.7e-10 (base qualities <= 93); a read with a higher quality
+        // (up to 255: 0xFF marks a missing quality string) is left undecided for the exact replay
+        int qmax = 0;
 
         // ---- forward, row 1: slot s = cell k, band [1, min(refLen, bw + 1)] ----
         float fM[NS], fI[NS], fD[NS];
@@ -177,6 +180,7 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
             const int end = refLen < bw + 1 ? refLen : bw + 1;
             const bool act = qL >= 1;
             const u8 q0 = act ? QRY(0) : 0, qq0 = act ? QUL(0) : 0;
+            qmax = qq0;
             float part = 0.0f;
 #pragma unroll
             for (int j = 0; j < NS; j++) {
@@ -218,6 +222,7 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
             const int x = i - bw > 0 ? i - bw : 0;
             const bool slide = i > bw;
             const u8 qy = act ? QRY(i - 1) : 0, qq = act ? QUL(i - 1) : 0;
+            qmax = qmax > qq ? qmax : qq;
             // the D chain visits only the slots holding band cells of some group (zeros elsewhere)
             const int slo = int(__reduce_min_sync(FULL, u32(act ? (beg - x > 0 ? beg - x : 0) : WC)));
             const int shi = int(__reduce_max_sync(FULL, u32(act ? (end - x < WC - 1 ? end - x : WC - 1) : 0)));
@@ -518,6 +523,8 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
                 w.baq_amb[qi] = amb;
             }
         }
+        if (has && qmax > 93)
+            for (int row = l; row < qL; row += G) w.baq_amb[qual0 + u32(row)] = 7;
         __syncwarp();
     }
 }

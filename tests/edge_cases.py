@@ -1,6 +1,7 @@
 """Hand-built alignment batch covering the reference's special cases: every read filter, clip layouts,
-leading/trailing insertions, deletions, '=' and X ops, N bases, low-quality tails, reads at both contig
-ends, adapter clipping of short fragments, wide bands, known sites under reads, and malformed input."""
+leading/trailing insertions, deletions, '=' and X ops, N bases, low-quality tails, qualities above 93, reads at
+both contig ends, adapter clipping of short fragments, wide bands, known sites under reads, and malformed
+input."""
 from __future__ import annotations
 
 import re
@@ -160,6 +161,11 @@ def edge_case_dataset(seed=11):
     add(1650, "511M", subs=(100, 300, 500)) if L > 2200 else None
     add(1800, "70M", subs=(35,), rg=1)
     add(1850, "70M", subs=(35,), rg=2, flags=REV)
+    # base qualities above 93 (emissions below the FP32 kernels' range arguments; 0xFF = missing qualities):
+    # band classes 0, 1 and 2
+    add(2250, "50M", subs=(10, 30), quals=[255] * 50)
+    add(2320, "30M3D20M", subs=(5,), quals=[120] * 50)
+    add(2400, "25M20D25M", subs=(3, 40), quals=[93] * 20 + [200] * 30)
 
     # known sites: SNPs under reads 0, 5, 9; an indel site; a site at the read edge
     sites = sorted([(110, 110), (130, 130), (215, 215), (245, 247), (289, 289), (1010, 1012), (1220, 1220),
