@@ -10,3 +10,38 @@ def test_fractional_error_division_single_rounding():
     via_double = (n / ln).astype(np.float32)
     direct = n.astype(np.float32) / ln.astype(np.float32)
     assert int((via_double != direct).sum()) == 0
+
+
+def test_fp32_baq_range_arguments():
+    """The FP32 BAQ kernels' range arguments, in float32 arithmetic: with base qualities <= 93 (higher ones go
+    to the exact replay) every emission is >= 1.67e-10, and
+    - band class 0: a stored value >= 1e-22 times any factor chain of the next row (emission, gap-open
+      transition, 0.1 extension, insertion emission 0.25) stays a normal float;
+    - flush-and-bound (classes 1 and 2): operands >= 2^-78 keep every product and sum of a row normal, and a
+      flushed value's absolute error, carried through the row scaling, stays far below the 2^-24 slack."""
+    tiny = np.float32(np.finfo(np.float32).tiny)  # 2^-126
+    q = np.arange(0, 94)
+    p = 10.0 ** (-np.maximum(q, 4) / 10.0)
+    e_mis = (p * 0.33333333333).astype(np.float32)
+    e_match = (1 - p).astype(np.float32)
+    e_min = min(e_mis.min(), e_match.min())
+    assert e_min >= np.float32(1.6e-10)
+    gop = 10.0 ** (-4.0)
+    ds_max = 1.0 / (2 * 1 + 2)  # qL >= 1
+    m2_min = np.float32(gop * (1 - ds_max))  # gap open (and m1)
+    # class 0: one row of products from a stored value >= 1e-22 (the D chain of the same row adds m2 then 0.1 steps
+    # whose values are stored or rescaled within the row sum)
+    v = np.float32(1e-22) * e_min * np.float32(0.9) * m2_min
+    assert v >= tiny
+    # flush-and-bound: every operand is 0 or >= 2^-78, and a computed cell is flushed before it feeds another
+    # cell, so the products of a row are at most two factors deep on a kept operand: emission x transition
+    # (M, and the backward e = emission x B_M then x m0 / m3 / m6), EI x m1 or m4 (I), m2 x M and m8 x D (the D
+    # chains)
+    flush = np.float32(2.0 ** -78)
+    m_min = min(np.float32((1 - 2 * gop) * (1 - ds_max)), np.float32(0.9 * (1 - ds_max)), np.float32(0.9))
+    chains = [flush * e_min * m_min, flush * np.float32(0.25) * m2_min, flush * m2_min, flush * np.float32(0.1)]
+    assert min(chains) >= tiny
+    assert min(chains) >= np.float32(2.0 ** -112)
+    assert float(flush) == 3.3087224502121107e-24
+    # posterior terms of two kept values may underflow: 2^-150 each at most, far below a row sum >= 2^0
+    assert 2 * 63 * 2.0 ** -150 < 2.0 ** -24
