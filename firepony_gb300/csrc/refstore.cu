@@ -186,10 +186,14 @@ struct fp_refstore {
         }
         return off;
     }
-    u64 image_bytes() const {
+    u64 image_bytes() const {  // (allocates nothing)
         if (mapped) return map_bytes;
-        std::vector<DirEntry> d;
-        return layout(d);
+        u64 off = align_up(sizeof(ImageHeader) + sizeof(DirEntry) * u64(nc));
+        for (u32 i = 0; i < nc; i++) {
+            off = align_up(off + u64(words[i].size()) * 4);
+            if (!sites[i].empty()) off = align_up(off + u64(sites[i].size()) * 4);
+        }
+        return off;
     }
     // writes a built store's image into `dst` (image_bytes() bytes, zero-filled); the ready mark is left 0
     void write_image(u8 *dst) const {
@@ -377,7 +381,12 @@ fp_status fp_refstore_publish(const fp_refstore *cs, const char *name) {
         memcpy(dst, s->map, bytes);
         reinterpret_cast<ImageHeader *>(dst)->ready = 0;
     } else {
-        s->write_image(dst);
+        try {
+            s->write_image(dst);
+        } catch (...) {
+            munmap(p, bytes);
+            return undo(FP_OOM, "image directory");
+        }
     }
     __atomic_store_n(&reinterpret_cast<ImageHeader *>(dst)->ready, READY, __ATOMIC_RELEASE);
     munmap(p, bytes);
