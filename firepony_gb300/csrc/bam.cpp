@@ -223,9 +223,19 @@ const char *find_rg(const uint8_t *p, const uint8_t *end, size_t &len) {
 
 extern "C" {
 
+static int open_impl(const char *path, int threads, fpb_reader **out);
+
 int fpb_open(const char *path, int threads, fpb_reader **out) {
     if (!path || !out) return -1;
     *out = nullptr;
+    try {  // (no C++ exception crosses the C ABI)
+        return open_impl(path, threads, out);
+    } catch (...) {
+        return -1;
+    }
+}
+
+static int open_impl(const char *path, int threads, fpb_reader **out) {
     fpb_reader *r = new fpb_reader();
     r->threads = threads > 0 ? threads : int(std::max(1u, std::thread::hardware_concurrency()));
     r->f = fopen(path, "rb");
@@ -290,7 +300,13 @@ int64_t fpb_next_batch(fpb_reader *r, uint32_t max_reads, fp_batch_view *v) {
         return -1;
     }
     const double t0 = now_s(), read0 = r->stats.seconds_read;
-    const int64_t n = next_batch_host(r, max_reads, v);
+    int64_t n;
+    try {  // (no C++ exception crosses the C ABI)
+        n = next_batch_host(r, max_reads, v);
+    } catch (...) {
+        r->err.assign("host alloc fail");
+        n = -1;
+    }
     r->stats.seconds_decode += (now_s() - t0) - (r->stats.seconds_read - read0);
     if (n < 0 && r->mode == 1 && !r->failed) {  // (a call in the wrong mode leaves the reader usable)
         r->failed = true;
@@ -503,10 +519,27 @@ int reg2bin(int beg, int end) {
 
 }  // namespace
 
+static int write_bam_impl(const char *path, uint32_t num_targets, const char *const *target_names,
+                          const uint32_t *target_lengths, uint32_t num_read_groups,
+                          const char *const *read_group_ids, const fp_batch_view *batches, uint32_t num_batches,
+                          int level, int threads);
+
 extern "C" int fpb_write_bam(const char *path, uint32_t num_targets, const char *const *target_names,
                              const uint32_t *target_lengths, uint32_t num_read_groups,
                              const char *const *read_group_ids, const fp_batch_view *batches, uint32_t num_batches,
                              int level, int threads) {
+    try {  // (no C++ exception crosses the C ABI)
+        return write_bam_impl(path, num_targets, target_names, target_lengths, num_read_groups, read_group_ids,
+                              batches, num_batches, level, threads);
+    } catch (...) {
+        return -1;
+    }
+}
+
+static int write_bam_impl(const char *path, uint32_t num_targets, const char *const *target_names,
+                          const uint32_t *target_lengths, uint32_t num_read_groups,
+                          const char *const *read_group_ids, const fp_batch_view *batches, uint32_t num_batches,
+                          int level, int threads) {
     if (!path || (num_targets && (!target_names || !target_lengths)) || (num_read_groups && !read_group_ids))
         return -1;
     const int nt = threads > 0 ? threads : int(std::max(1u, std::thread::hardware_concurrency()));

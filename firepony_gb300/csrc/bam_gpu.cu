@@ -1019,7 +1019,13 @@ extern "C" int64_t fpb_next_batch_device(fpb_reader *r, uint32_t max_reads, fp_b
         return -1;
     }
     const double t0 = now_s(), read0 = r->stats.seconds_read;
-    const int64_t n = next_batch_device(r, max_reads, v);
+    int64_t n;
+    try {  // (no C++ exception crosses the C ABI)
+        n = next_batch_device(r, max_reads, v);
+    } catch (...) {
+        r->err.assign("host alloc fail");
+        n = -1;
+    }
     r->stats.seconds_decode += (now_s() - t0) - (r->stats.seconds_read - read0);
     if (n < 0 && r->mode == 2 && !r->failed) {  // (a call in the wrong mode leaves the reader usable)
         r->failed = true;

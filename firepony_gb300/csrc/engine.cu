@@ -211,11 +211,25 @@ fp_status upload_refs(fp_engine *eng) {
     return FP_OK;
 }
 
+// C entry points return a status for host allocation failures and other C++ exceptions instead of letting
+// them cross the C ABI (which would terminate the caller's process)
+template <typename F> fp_status guarded(fp_engine *eng, F &&body) {
+    try {
+        return body();
+    } catch (const std::bad_alloc &) {
+        if (eng) eng->err.assign("host alloc failed");
+        return FP_OOM;
+    } catch (...) {
+        if (eng) eng->err.assign("host exception");
+        return FP_DEVICE_ERROR;
+    }
+}
+
 }  // namespace
 
 extern "C" {
 
-fp_status fp_engine_create(const fp_options *o, fp_engine **out) {
+static fp_status create_impl(const fp_options *o, fp_engine **out) {
     if (!o || !out) return FP_BAD_INPUT;
     *out = nullptr;
     if (o->num_read_groups == 0 || o->num_read_groups > 256) return FP_BAD_INPUT;
@@ -348,8 +362,8 @@ fp_status fp_engine_set_contig(fp_engine *eng, uint32_t id, const uint32_t *pack
     return upload_refs(eng);
 }
 
-fp_status fp_engine_set_known_sites(fp_engine *eng, uint32_t id, const uint32_t *start, const uint32_t *stop,
-                                    uint32_t n) {
+static fp_status set_known_sites_impl(fp_engine *eng, uint32_t id, const uint32_t *start, const uint32_t *stop,
+                                       uint32_t n) {
     if (!eng || ((!start || !stop) && n)) return FP_BAD_INPUT;
     if (eng->store) return eng->fail(FP_BAD_INPUT, "the engine reads an attached reference store");
     CK(cudaSetDevice(eng->device), "set device");
@@ -381,7 +395,7 @@ static fp_status co_flush(fp_engine *eng);
 // Engines of one GPU share a reference store's device copy (segmented_database.h:224-244 keeps one resident
 // set per engine). The engine's own contigs and sites are freed; work already queued is finished first, and
 // host batches staged for coalescing are submitted under the reference they were staged with.
-fp_status fp_engine_attach_refstore(fp_engine *eng, fp_refstore *store) {
+static fp_status attach_refstore_impl(fp_engine *eng, fp_refstore *store) {
     if (!eng) return FP_BAD_INPUT;
     if (store == eng->store) return FP_OK;
     CK(cudaSetDevice(eng->device), "set device");
@@ -457,7 +471,7 @@ static fp_status stage_inputs(fp_engine *eng, int k, const fp_batch_view *v, con
     return FP_OK;
 }
 
-fp_status fp_engine_prefetch_batch(fp_engine *eng, const fp_batch_view *v) {
+static fp_status prefetch_batch_impl(fp_engine *eng, const fp_batch_view *v) {
     if (!eng || !v) return FP_BAD_INPUT;
     if (v->num_reads == 0) return FP_OK;
     if (eng->co_target) return FP_OK;  // coalescing copies each batch into the staging batch at its submit
@@ -480,12 +494,12 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device);
 static fp_status co_submit(fp_engine *eng, const fp_batch_view *v);
 static fp_status co_flush(fp_engine *eng);
 
-fp_status fp_engine_submit_batch(fp_engine *eng, const fp_batch_view *v) {
+static fp_status submit_batch_impl(fp_engine *eng, const fp_batch_view *v) {
     if (eng && v && eng->co_target) return co_submit(eng, v);
     return submit(eng, v, false);
 }
 
-fp_status fp_engine_submit_batch_device(fp_engine *eng, const fp_batch_view *v) {
+static fp_status submit_batch_device_impl(fp_engine *eng, const fp_batch_view *v) {
     if (eng && eng->co_target) {
         const fp_status s = co_flush(eng);  // staged reads come first in stream order
         if (s != FP_OK) return s;
@@ -1007,7 +1021,7 @@ static fp_status co_submit(fp_engine *eng, const fp_batch_view *v) {
 
 extern "C" {
 
-fp_status fp_engine_finalize(fp_engine *eng) {
+static fp_status finalize_impl(fp_engine *eng) {
     if (!eng) return FP_BAD_INPUT;
     CK(cudaSetDevice(eng->device), "set device");
     if (eng->co_target && !eng->finalized) {
@@ -1166,8 +1180,8 @@ fp_status fp_engine_get_table(fp_engine *eng, int32_t id, fp_table_view *out) {
     return FP_OK;
 }
 
-fp_status fp_engine_write_report(fp_engine *eng, const char *path, const char *const *rg_names, uint32_t num_rg_names,
-                                 int disable_rounding, int vmaj, int vmin, int vrev) {
+static fp_status write_report_impl(fp_engine *eng, const char *path, const char *const *rg_names,
+                                   uint32_t num_rg_names, int disable_rounding, int vmaj, int vmin, int vrev) {
     if (!eng) return FP_BAD_INPUT;
     if (!eng->finalized) return eng->fail(FP_NOT_READY, "write_report needs fp_engine_finalize first");
     fp_table_view t[4];
@@ -1203,8 +1217,8 @@ fp_status fp_engine_get_stats(const fp_engine *eng, fp_stats *out) {
     return FP_OK;
 }
 
-fp_status fp_engine_debug_last_batch(fp_engine *eng, uint8_t *read_status, uint16_t *windows, int16_t *hmm,
-                                     uint8_t *base_flags, uint8_t *baq_tag, double *frac_errors) {
+static fp_status debug_last_batch_impl(fp_engine *eng, uint8_t *read_status, uint16_t *windows, int16_t *hmm,
+                                       uint8_t *base_flags, uint8_t *baq_tag, double *frac_errors) {
     if (!eng) return FP_BAD_INPUT;
     CK(cudaSetDevice(eng->device), "set device");
     CK(cudaStreamSynchronize(eng->st), "debug");
@@ -1243,6 +1257,54 @@ fp_status fp_host_alloc(size_t bytes, void **out) {
 
 void fp_host_free(void *p) {
     if (p) cudaFreeHost(p);
+}
+
+}  // extern "C"
+
+// ---- C entry points that allocate host memory, guarded (see `guarded`) ----
+extern "C" {
+
+fp_status fp_engine_set_known_sites(fp_engine *eng, uint32_t id, const uint32_t *start, const uint32_t *stop,
+                                    uint32_t n) {
+    return guarded(eng, [&] { return set_known_sites_impl(eng, id, start, stop, n); });
+}
+
+fp_status fp_engine_attach_refstore(fp_engine *eng, fp_refstore *store) {
+    return guarded(eng, [&] { return attach_refstore_impl(eng, store); });
+}
+
+fp_status fp_engine_prefetch_batch(fp_engine *eng, const fp_batch_view *v) {
+    return guarded(eng, [&] { return prefetch_batch_impl(eng, v); });
+}
+
+fp_status fp_engine_submit_batch(fp_engine *eng, const fp_batch_view *v) {
+    return guarded(eng, [&] { return submit_batch_impl(eng, v); });
+}
+
+fp_status fp_engine_submit_batch_device(fp_engine *eng, const fp_batch_view *v) {
+    return guarded(eng, [&] { return submit_batch_device_impl(eng, v); });
+}
+
+fp_status fp_engine_finalize(fp_engine *eng) {
+    return guarded(eng, [&] { return finalize_impl(eng); });
+}
+
+fp_status fp_engine_write_report(fp_engine *eng, const char *path, const char *const *rg_names, uint32_t num_rg_names,
+                                 int disable_rounding, int vmaj, int vmin, int vrev) {
+    return guarded(eng, [&] {
+        return write_report_impl(eng, path, rg_names, num_rg_names, disable_rounding, vmaj, vmin, vrev);
+    });
+}
+
+fp_status fp_engine_debug_last_batch(fp_engine *eng, uint8_t *read_status, uint16_t *windows, int16_t *hmm,
+                                     uint8_t *base_flags, uint8_t *baq_tag, double *frac_errors) {
+    return guarded(eng, [&] {
+        return debug_last_batch_impl(eng, read_status, windows, hmm, base_flags, baq_tag, frac_errors);
+    });
+}
+
+fp_status fp_engine_create(const fp_options *o, fp_engine **out) {
+    return guarded(nullptr, [&] { return create_impl(o, out); });
 }
 
 }  // extern "C"

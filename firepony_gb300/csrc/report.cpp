@@ -132,10 +132,27 @@ const std::string &rg_name(const char *const *names, uint32_t n, uint32_t id, st
 
 }  // namespace
 
+static fp_status report_write(FILE *f, const fp_table_view *tables, const char *const *rg_names,
+                              uint32_t num_rg_names, int disable_rounding, int vmaj, int vmin, int vrev);
+
+// The writer's strings and vectors may fail to allocate: that is reported as FP_OOM (with the file closed),
+// never as an exception through the C ABI.
 extern "C" fp_status fp_report_write(const char *path, const fp_table_view *tables, const char *const *rg_names,
                                      uint32_t num_rg_names, int disable_rounding, int vmaj, int vmin, int vrev) {
     FILE *f = (path && *path) ? fopen(path, "w") : stdout;
     if (!f) return FP_BAD_INPUT;
+    fp_status st;
+    try {
+        st = report_write(f, tables, rg_names, num_rg_names, disable_rounding, vmaj, vmin, vrev);
+    } catch (...) {
+        if (f != stdout) fclose(f);
+        return FP_OOM;
+    }
+    return st;
+}
+
+static fp_status report_write(FILE *f, const fp_table_view *tables, const char *const *rg_names,
+                              uint32_t num_rg_names, int disable_rounding, int vmaj, int vmin, int vrev) {
     const bool raw = disable_rounding != 0;
     // header and Arguments table (device/pipeline.cu:150-178)
     fputs("#:GATKReport.v1.1:5\n", f);
