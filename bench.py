@@ -596,6 +596,17 @@ def roofline(res, args):
                         "note": "binding roofline: FP32 SIMT issue; forward rows spill to HBM scratch"}}
 
 
+def _leg(fn, *a):
+    """An auxiliary measurement: its failure is reported in its own field (traceback on stderr) instead of
+    ending the run before the headline line is printed."""
+    try:
+        return fn(*a)
+    except Exception as ex:  # noqa: BLE001 - any failure of a side measurement
+        import traceback
+        traceback.print_exc()
+        return {"error": f"{type(ex).__name__}: {ex}"}
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -645,13 +656,13 @@ def main():
         cpu = None
         if not args.no_cpu_baseline and world == 1:
             cpu = cpu_baseline(res["ref"], res["batches"], args.cpu_sample_seconds)
-        plain = run_plain(args, res) if args.plain_steps > 0 and world == 1 and args.baq == "fp32" else None
-        serving = run_serving(args) if args.serve_jobs > 0 and world == 1 else None
-        bam_in = run_bam(args, res) if args.bam_batches > 0 and world == 1 else None
-        batched = run_batched(args) if args.batched_batches > 0 and world == 1 else None
-        configs = run_config_legs(args) if args.config_legs and world == 1 else None
-        refstore = run_refstore(args) if not args.no_refstore and world == 1 else None
-        sort = run_sort(args) if args.sort_entries > 0 and world == 1 else None
+        plain = _leg(run_plain, args, res) if args.plain_steps > 0 and world == 1 and args.baq == "fp32" else None
+        serving = _leg(run_serving, args) if args.serve_jobs > 0 and world == 1 else None
+        bam_in = _leg(run_bam, args, res) if args.bam_batches > 0 and world == 1 else None
+        batched = _leg(run_batched, args) if args.batched_batches > 0 and world == 1 else None
+        configs = _leg(run_config_legs, args) if args.config_legs and world == 1 else None
+        refstore = _leg(run_refstore, args) if not args.no_refstore and world == 1 else None
+        sort = _leg(run_sort, args) if args.sort_entries > 0 and world == 1 else None
         line = {"metric": METRIC, "value": value, "unit": "reads/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
