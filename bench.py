@@ -655,7 +655,7 @@ def main():
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline and world == 1:
-            cpu = cpu_baseline(res["ref"], res["batches"], args.cpu_sample_seconds)
+            cpu = _leg(cpu_baseline, res["ref"], res["batches"], args.cpu_sample_seconds)
         plain = _leg(run_plain, args, res) if args.plain_steps > 0 and world == 1 and args.baq == "fp32" else None
         serving = _leg(run_serving, args) if args.serve_jobs > 0 and world == 1 else None
         bam_in = _leg(run_bam, args, res) if args.bam_batches > 0 and world == 1 else None
