@@ -109,7 +109,13 @@ constexpr int RS_ROUNDS = 16;
 constexpr int RS_WARP_KEYS = 32 * RS_ROUNDS;
 constexpr int RS_TILE = RS_THREADS * RS_ROUNDS;
 
-__device__ __forceinline__ u32 digit_of(u64 v, int shift) { return u32(v >> (32 + shift)) & 0xFFu; }
+// The digit of a pass: key bits [shift, shift + 8) of the entry, cut at key_bits so that key bits above the
+// sorted width never decide the order (the last pass of a width that is not a multiple of 8 takes fewer bits).
+__device__ __forceinline__ u32 digit_mask(int shift, int key_bits) {
+    const int w = key_bits - shift;
+    return w >= 8 ? 0xFFu : ((1u << w) - 1u);
+}
+__device__ __forceinline__ u32 digit_of(u64 v, int shift, u32 mask) { return u32(v >> (32 + shift)) & mask; }
 
 // The lanes of the warp holding a key with digit d (the caller's own lane included), from one ballot per digit
 // bit; lanes without a key form their own group. Votes run on the integer pipe, where a match instruction
@@ -126,7 +132,9 @@ __device__ __forceinline__ u32 digit_peers(u32 d, bool valid) {
     return peers;
 }
 
-__global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const u64 *in, u64 n, int shift, u32 *hist, u32 nblocks) {
+__global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const u64 *in, u64 n, int shift, int key_bits, u32 *hist,
+                                                        u32 nblocks) {
+    const u32 dmask = digit_mask(shift, key_bits);
     __shared__ u32 h[RS_WARPS][256];  // per warp: only its own lanes update it
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int j = threadIdx.x; j < RS_WARPS * 256; j += RS_THREADS) (&h[0][0])[j] = 0;
@@ -141,7 +149,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const u64 *in, u64 n, in
 #pragma unroll
     for (int r = 0; r < RS_ROUNDS; r++) {
         const bool valid = wbase + u64(r) * 32 + lane < n;
-        const u32 d = digit_of(v[r], shift);
+        const u32 d = digit_of(v[r], shift, dmask);
         const u32 peers = digit_peers(d, valid);
         // one update per distinct digit (distinct addresses within the instruction)
         if (valid && int(__ffs(peers)) - 1 == lane) h[warp][d] += u32(__popc(peers));
@@ -154,8 +162,9 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const u64 *in, u64 n, in
     hist[u64(threadIdx.x) * nblocks + blockIdx.x] = t;
 }
 
-__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const u64 *in, u64 n, int shift, const u32 *offs,
-                                                           u32 nblocks, u64 *out) {
+__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const u64 *in, u64 n, int shift, int key_bits,
+                                                           const u32 *offs, u32 nblocks, u64 *out) {
+    const u32 dmask = digit_mask(shift, key_bits);
     __shared__ u64 buf[RS_TILE];            // the tile ordered by digit
     __shared__ u32 wcnt[RS_WARPS][256];     // per warp: digit counts, then the warp's first slot per digit
     __shared__ u32 tstart[256];             // first slot of each digit in the ordered tile
@@ -177,7 +186,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const u64 *in, u64 n,
 #pragma unroll
     for (int r = 0; r < RS_ROUNDS; r++) {
         const bool valid = wbase + u64(r) * 32 + lane < n;
-        const u32 d = digit_of(v[r], shift);
+        const u32 d = digit_of(v[r], shift, dmask);
         const u32 peers = digit_peers(d, valid);
         const u32 before = valid ? wcnt[warp][d] : 0u;  // the digit's peers read one word together
         const u32 rk = before + u32(__popc(peers & lt));
@@ -208,13 +217,13 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const u64 *in, u64 n,
 #pragma unroll
     for (int r = 0; r < RS_ROUNDS; r++) {
         const u64 i = wbase + u64(r) * 32 + lane;
-        if (i < n) buf[wcnt[warp][digit_of(v[r], shift)] + ((rank[r >> 1] >> ((r & 1) * 16)) & 0xFFFFu)] = v[r];
+        if (i < n) buf[wcnt[warp][digit_of(v[r], shift, dmask)] + ((rank[r >> 1] >> ((r & 1) * 16)) & 0xFFFFu)] = v[r];
     }
     __syncthreads();
     const u32 tile_n = u32(n - tile0 < u64(RS_TILE) ? n - tile0 : u64(RS_TILE));
     for (u32 p = threadIdx.x; p < tile_n; p += RS_THREADS) {
         const u64 key = buf[p];
-        const u32 d = digit_of(key, shift);
+        const u32 d = digit_of(key, shift, dmask);
         out[gbase[d] + (p - tstart[d])] = key;
     }
 }
@@ -292,9 +301,9 @@ void launch_radix_sort(u64 *keys, u64 *alt, u64 n, int key_bits, void *tmp, size
         u32 *offs = hist + hist_n + 1;
         void *stmp = offs + hist_n + 1;
         for (int shift = 0; shift < key_bits; shift += 8) {
-            k_rs_hist<<<nblocks, RS_THREADS, 0, s>>>(src, n, shift, hist, nblocks);
+            k_rs_hist<<<nblocks, RS_THREADS, 0, s>>>(src, n, shift, key_bits, hist, nblocks);
             scan_rec(hist, offs, hist_n, reinterpret_cast<u32 *>(stmp), s);
-            k_rs_scatter<<<nblocks, RS_THREADS, 0, s>>>(src, n, shift, offs, nblocks, dst);
+            k_rs_scatter<<<nblocks, RS_THREADS, 0, s>>>(src, n, shift, key_bits, offs, nblocks, dst);
             g_kernel_launches += 2;
             u64 *t = src;
             src = dst;
@@ -342,9 +351,9 @@ void sort_into(const u64 *in, u64 *out, u64 *alt, u64 n, int key_bits, void *tmp
     for (int shift = 0; shift < key_bits; shift += 8, p++) {
         // pass p writes `out` when the number of passes left (passes - p) is odd
         u64 *dst = ((passes - p) % 2 == 1) ? out : alt;
-        k_rs_hist<<<nblocks, RS_THREADS, 0, s>>>(src, n, shift, hist, nblocks);
+        k_rs_hist<<<nblocks, RS_THREADS, 0, s>>>(src, n, shift, key_bits, hist, nblocks);
         scan_rec(hist, offs, hist_n, reinterpret_cast<u32 *>(stmp), s);
-        k_rs_scatter<<<nblocks, RS_THREADS, 0, s>>>(src, n, shift, offs, nblocks, dst);
+        k_rs_scatter<<<nblocks, RS_THREADS, 0, s>>>(src, n, shift, key_bits, offs, nblocks, dst);
         g_kernel_launches += 2;
         src = dst;
     }
@@ -358,6 +367,7 @@ extern "C" fp_status fp_sort_entries(const uint64_t *d_in, uint64_t *d_out, uint
     using namespace fpg;
     if ((!d_in || !d_out) && n) return FP_BAD_INPUT;
     if (key_bits < 0 || key_bits > 32) return FP_BAD_INPUT;
+    if (n > FP_SORT_MAX_ENTRIES) return FP_BAD_INPUT;  // digit counts and offsets are 32-bit
     if (n == 0) return FP_OK;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     const size_t tmp_bytes = radix_tmp_bytes(n);

@@ -221,9 +221,13 @@ fp_status fp_engine_debug_last_batch(fp_engine *engine, uint8_t *read_status, ui
 
 /* Stable LSD radix sort of n packed 64-bit covariate entries (key in bits 32..63, payload below) by key
  * bits [32, 32 + key_bits), device pointers in and out (d_in is not modified; the ranges must not
- * overlap). The engine's K4 sort, exposed for callers that build their own entry streams, in the role of
+ * overlap). Key bits at and above key_bits do not take part: entries that differ only there keep their
+ * input order. The engine's K4 sort, exposed for callers that build their own entry streams, in the role of
  * covariate_table::sort (device/covariate_table.cu:43-57). Runs on `stream` (a cudaStream_t, NULL for the
- * default stream) and returns once the work is queued; scratch is allocated and freed on that stream. */
+ * default stream) and returns once the work is queued; scratch is allocated and freed on that stream.
+ * n may be at most FP_SORT_MAX_ENTRIES (digit counts and offsets are 32-bit); larger n returns
+ * FP_BAD_INPUT. */
+#define FP_SORT_MAX_ENTRIES 0xFFFFFFFEull
 fp_status fp_sort_entries(const uint64_t *d_in, uint64_t *d_out, uint64_t n, int key_bits, void *stream);
 
 /* fp_sort_entries without any device allocation, for callers that must not allocate while they run (a

@@ -104,26 +104,59 @@ struct ObsTable {
     std::vector<TableRow> rows;
 
     // Appends entries (in stream order), stable-sorts by key and reduces with a left fold
-    // (device/covariates.cu:172-201, device/covariate_table.cu:43-107).
+    // (device/covariates.cu:172-201, device/covariate_table.cu:43-107). fold_sorted takes entries already in
+    // that stable order.
     void fold(std::vector<Entry> &entries) {
-        if (entries.empty()) return;
         std::stable_sort(entries.begin(), entries.end(), [](const Entry &a, const Entry &b) { return a.key < b.key; });
-        std::vector<TableRow> out;
-        out.reserve(rows.size() + entries.size());
-        size_t i = 0, j = 0;
-        while (i < rows.size() || j < entries.size()) {
+        fold_sorted(entries);
+    }
+    void fold_sorted(const std::vector<Entry> &entries, int num_threads = 1) {
+        if (entries.empty()) return;
+        // the key range is cut at entry keys into parts that never split a key; each part merges the running
+        // rows and the new entries of its keys on its own thread, and the parts are concatenated in order
+        const int P = std::max(1, std::min<int>(num_threads, int(entries.size() / 4096) + 1));
+        std::vector<size_t> ecut(P + 1), rcut(P + 1);
+        ecut[0] = 0; rcut[0] = 0; ecut[P] = entries.size(); rcut[P] = rows.size();
+        for (int p = 1; p < P; p++) {
+            const u32 k = entries[entries.size() * p / P].key;
+            ecut[p] = size_t(std::lower_bound(entries.begin(), entries.end(), k,
+                                              [](const Entry &e, u32 x) { return e.key < x; }) - entries.begin());
+            rcut[p] = size_t(std::lower_bound(rows.begin(), rows.end(), k,
+                                              [](const TableRow &r, u32 x) { return r.key < x; }) - rows.begin());
+        }
+        // (the part and output buffers are kept from batch to batch so their pages are reused)
+        if (part_buf.size() < size_t(P)) part_buf.resize(size_t(P));
+#pragma omp parallel for num_threads(P) schedule(static, 1) if (P > 1)
+        for (int p = 0; p < P; p++) {
+            part_buf[p].clear();
+            merge_range(rows, rcut[p], rcut[p + 1], entries, ecut[p], ecut[p + 1], part_buf[p]);
+        }
+        spare.clear();
+        size_t n = 0;
+        for (int p = 0; p < P; p++) n += part_buf[p].size();
+        spare.reserve(n);
+        for (int p = 0; p < P; p++) spare.insert(spare.end(), part_buf[p].begin(), part_buf[p].end());
+        rows.swap(spare);
+    }
+    std::vector<TableRow> spare;
+    std::vector<std::vector<TableRow>> part_buf;
+
+    static void merge_range(const std::vector<TableRow> &rows, size_t i, size_t i_end, const std::vector<Entry> &entries,
+                            size_t j, size_t j_end, std::vector<TableRow> &out) {
+        out.reserve((i_end - i) + (j_end - j));
+        while (i < i_end || j < j_end) {
             u32 key;
-            if (j >= entries.size() || (i < rows.size() && rows[i].key <= entries[j].key)) key = rows[i].key;
+            if (j >= j_end || (i < i_end && rows[i].key <= entries[j].key)) key = rows[i].key;
             else key = entries[j].key;
             TableRow acc = {key, 0, 0.0f};
             bool first = true;
             // the running row precedes the new entries of the same key (stable order)
-            if (i < rows.size() && rows[i].key == key) {
+            if (i < i_end && rows[i].key == key) {
                 acc = rows[i];
                 first = false;
                 i++;
             }
-            while (j < entries.size() && entries[j].key == key) {
+            while (j < j_end && entries[j].key == key) {
                 if (first) {
                     acc.observations = 1;
                     acc.mismatches = entries[j].mism;
@@ -136,7 +169,6 @@ struct ObsTable {
             }
             out.push_back(acc);
         }
-        rows.swap(out);
     }
 };
 
@@ -419,6 +451,9 @@ struct fpo_ctx {
     std::vector<u64> out_obs[4];
     std::vector<double> out_mism[4], out_exp[4], out_est[4], out_emp[4];
     u64 total_reads = 0, filtered_reads = 0, baq_reads = 0, num_batches = 0;
+    // thread-seconds per stage (FPO_STAGE_*), summed over the OpenMP threads
+    double stage_sec[FPO_NUM_STAGES] = {};
+    std::vector<std::vector<Entry>> run_q, run_c, run_x;  // per-chunk entry streams of a batch
     double qual2prob[256];
     double gap_open;
 
@@ -1249,6 +1284,18 @@ void gather_event(const BatchState &s, u32 e, std::vector<Entry> *outq, std::vec
     }
 }
 
+// Thread-seconds per stage: lap(k) charges the time since the previous lap (or start) to stage k.
+struct StageClock {
+    double sec[FPO_NUM_STAGES] = {};
+    double last = 0.0;
+    void start() { last = omp_get_wtime(); }
+    void lap(int k) {
+        const double now = omp_get_wtime();
+        sec[k] += now - last;
+        last = now;
+    }
+};
+
 int resolve_threads(int n) {
 #ifdef _OPENMP
     return n > 0 ? n : omp_get_max_threads();
@@ -1326,24 +1373,32 @@ int fpo_process_batch(fpo_ctx *ctx, const fp_batch_view *b, int num_threads) {
     for (int t = 0; t < 3; t++) s.frac[t].assign(b->num_qualities, 0.0);
 
     u64 filtered = 0;
+    // per-thread stage clocks, merged into ctx->stage_sec at the end of each parallel region
+    std::vector<StageClock> clocks(static_cast<size_t>(nt));
     // filter_invalid_reads (device/read_filters.cu:262-336)
-#pragma omp parallel for num_threads(nt) schedule(static) reduction(+ : filtered)
-    for (u32 r = 0; r < R; r++) {
-        if (passes_invalid_filters(s, r)) {
-            s.status[r] = 1;
-        } else {
-            filtered++;
+#pragma omp parallel num_threads(nt)
+    {
+        StageClock &ck = clocks[size_t(omp_get_thread_num())];
+        ck.start();
+#pragma omp for schedule(static) reduction(+ : filtered)
+        for (u32 r = 0; r < R; r++) {
+            if (passes_invalid_filters(s, r)) {
+                s.status[r] = 1;
+            } else {
+                filtered++;
+            }
         }
-    }
-    // build_read_offset_list / build_alignment_windows / filter_malformed_reads (device/pipeline.cu:72-80)
-#pragma omp parallel for num_threads(nt) schedule(dynamic, 256) reduction(+ : filtered)
-    for (u32 r = 0; r < R; r++) {
-        if (!s.status[r]) continue;
-        alignment_window(s, r);
-        if (!passes_malformed_filter(ctx, s, r)) {
-            s.status[r] = 0;
-            filtered++;
+        // build_read_offset_list / build_alignment_windows / filter_malformed_reads (device/pipeline.cu:72-80)
+#pragma omp for schedule(dynamic, 256) reduction(+ : filtered)
+        for (u32 r = 0; r < R; r++) {
+            if (!s.status[r]) continue;
+            alignment_window(s, r);
+            if (!passes_malformed_filter(ctx, s, r)) {
+                s.status[r] = 0;
+                filtered++;
+            }
         }
+        ck.lap(FPO_STAGE_READ_FILTER);
     }
 
     // expand_cigars (device/cigar.cu:815-935)
@@ -1359,11 +1414,14 @@ int fpo_process_batch(fpo_ctx *ctx, const fp_batch_view *b, int num_threads) {
 #pragma omp parallel num_threads(nt)
     {
         HmmScratch scratch;
+        StageClock &ck = clocks[size_t(omp_get_thread_num())];
+        ck.start();
 #pragma omp for schedule(dynamic, 64)
         for (u32 r = 0; r < R; r++) {
             if (!s.status[r]) continue;
             expand_read(s, r);
         }
+        ck.lap(FPO_STAGE_CIGAR_EXPANSION);
 #pragma omp for schedule(dynamic, 64)
         for (u32 r = 0; r < R; r++) {
             if (!s.status[r]) continue;
@@ -1373,8 +1431,11 @@ int fpo_process_batch(fpo_ctx *ctx, const fp_batch_view *b, int num_threads) {
             no_insertions_window(s, r);
             reference_window(s, r);
             error_vectors(ctx, s, r);
+            ck.lap(FPO_STAGE_CIGAR_EXPANSION);
             filter_bases(s, r);
+            ck.lap(FPO_STAGE_BP_FILTER);
             filter_known_sites(ctx, s, r);
+            ck.lap(FPO_STAGE_SNP_FILTER);
             // baq_reads (device/baq.cu:1083-1336): windows for all active reads; reads needing BAQ whose
             // window leaves the contig lose their events. (Whether the batch filters them out of the
             // active list depends on other reads, but with their events cleared they contribute nothing.)
@@ -1387,56 +1448,100 @@ int fpo_process_batch(fpo_ctx *ctx, const fp_batch_view *b, int num_threads) {
                     s.ev_readc[i] = U16_NONE;
                 }
             }
+            ck.lap(FPO_STAGE_BAQ_SETUP);
         }
+        ck.lap(FPO_STAGE_CIGAR_EXPANSION);  // (waiting at the loop's barrier)
 #pragma omp for schedule(dynamic, 16) reduction(+ : baq_count)
         for (u32 r = 0; r < R; r++) {
             if (s.status[r] != 1) continue;
             const us2 w = s.clipped[r];
             if (s.num_errors[r] != 0) {
                 baq_read(ctx, s, r, scratch);
+                ck.lap(FPO_STAGE_BAQ_HMM);
                 cap_and_recode(s, r);
                 baq_count++;
             } else {
                 // read_flat_baq (:842-868)
                 memset(&s.baq[b->qual_start[r] + w.x], 64, u32(w.y - w.x + 1));
             }
+            ck.lap(FPO_STAGE_BAQ_POST);
             // build_fractional_error_arrays (device/fractional_errors.cu:119-141)
             fractional_errors(s, r, s.is_snp, s.frac[0]);
             fractional_errors(s, r, s.is_ins, s.frac[1]);
             fractional_errors(s, r, s.is_del, s.frac[2]);
+            ck.lap(FPO_STAGE_FRACTIONAL_ERROR);
             high_quality_window(s, r);
+            ck.lap(FPO_STAGE_COVARIATES_GATHER);
         }
+        ck.lap(FPO_STAGE_BAQ_HMM);  // (waiting at the loop's barrier)
     }
 
     // gather_covariates (device/covariates.cu:248-262): events in stream order into the three tables.
     // Reads are split into contiguous chunks; each chunk's entries keep stream order and chunks are
     // concatenated in order, so the result is independent of the thread count.
-    std::vector<std::vector<Entry>> cq(nt), cc(nt), cx(nt);
+    // per-chunk entry streams, kept in the context so their memory is reused from batch to batch
+    std::vector<std::vector<Entry>> &cq = ctx->run_q, &cc = ctx->run_c, &cx = ctx->run_x;
+    for (auto *v : {&cq, &cc, &cx}) {
+        v->resize(size_t(nt));
+        for (auto &run : *v) run.clear();
+    }
     std::vector<u32> chunk_start(nt + 1);
     for (int t = 0; t <= nt; t++) chunk_start[t] = u32(u64(R) * t / nt);
-#pragma omp parallel for num_threads(nt) schedule(static, 1)
-    for (int t = 0; t < nt; t++) {
-        for (u32 r = chunk_start[t]; r < chunk_start[t + 1]; r++) {
-            if (s.status[r] != 1) continue;
-            const u32 cs = s.cigar_offsets[b->cigar_start[r]];
-            const u32 ce = s.cigar_offsets[b->cigar_start[r] + b->cigar_len[r]];
-            for (u32 e = cs; e < ce; e++) gather_event(s, e, &cq[t], &cc[t], &cx[t]);
-        }
-    }
-    auto concat = [&](std::vector<std::vector<Entry>> &parts) {
-        std::vector<Entry> all;
-        size_t n = 0;
-        for (auto &p : parts) n += p.size();
-        all.reserve(n);
-        for (auto &p : parts) all.insert(all.end(), p.begin(), p.end());
-        return all;
-    };
+#pragma omp parallel num_threads(nt)
     {
-        std::vector<Entry> eq = concat(cq), ec = concat(cc), ex = concat(cx);
-        ctx->quality.fold(eq);
-        ctx->cycle.fold(ec);
-        ctx->context.fold(ex);
+        StageClock &ck = clocks[size_t(omp_get_thread_num())];
+        ck.start();
+#pragma omp for schedule(static, 1)
+        for (int t = 0; t < nt; t++) {
+            // the streams are filled through vectors on this thread's stack (the shared array of vector
+            // headers would put every append of neighbouring chunks on one cache line)
+            std::vector<Entry> lq, lc, lx;
+            lq.swap(cq[t]);
+            lc.swap(cc[t]);
+            lx.swap(cx[t]);
+            for (u32 r = chunk_start[t]; r < chunk_start[t + 1]; r++) {
+                if (s.status[r] != 1) continue;
+                const u32 cs = s.cigar_offsets[b->cigar_start[r]];
+                const u32 ce = s.cigar_offsets[b->cigar_start[r] + b->cigar_len[r]];
+                for (u32 e = cs; e < ce; e++) gather_event(s, e, &lq, &lc, &lx);
+            }
+            lq.swap(cq[t]);
+            lc.swap(cc[t]);
+            lx.swap(cx[t]);
+        }
+        ck.lap(FPO_STAGE_COVARIATES_GATHER);
     }
+    // The three tables' entry streams are stable-sorted in parallel: each chunk's run is sorted on its own
+    // thread, then runs are merged pairwise in chunk order (std::merge keeps equal keys of the earlier run
+    // first), which is the order a stable sort of the concatenation gives. The tables then fold side by side.
+    {
+        const double t0 = omp_get_wtime();
+        std::vector<std::vector<Entry>> *parts[3] = {&cq, &cc, &cx};
+        auto by_key = [](const Entry &a, const Entry &b) { return a.key < b.key; };
+#pragma omp parallel for num_threads(nt) schedule(dynamic, 1) collapse(2)
+        for (int tab = 0; tab < 3; tab++)
+            for (int t = 0; t < nt; t++) std::stable_sort((*parts[tab])[t].begin(), (*parts[tab])[t].end(), by_key);
+        for (int width = 1; width < nt; width *= 2) {
+            const int pairs = (nt + 2 * width - 1) / (2 * width);
+#pragma omp parallel for num_threads(nt) schedule(dynamic, 1) collapse(2)
+            for (int tab = 0; tab < 3; tab++) {
+                for (int pi = 0; pi < pairs; pi++) {
+                    const int a = pi * 2 * width, b2 = a + width;
+                    if (b2 >= nt) continue;
+                    std::vector<Entry> &ra = (*parts[tab])[a], &rb = (*parts[tab])[b2];
+                    std::vector<Entry> m(ra.size() + rb.size());
+                    std::merge(ra.begin(), ra.end(), rb.begin(), rb.end(), m.begin(), by_key);
+                    ra.swap(m);
+                    rb.clear();
+                }
+            }
+        }
+        ObsTable *tabs[3] = {&ctx->quality, &ctx->cycle, &ctx->context};
+        for (int tab = 0; tab < 3; tab++) tabs[tab]->fold_sorted((*parts[tab])[0], nt);
+        ctx->stage_sec[FPO_STAGE_COVARIATES_SORT_PACK] += omp_get_wtime() - t0;
+    }
+    for (const StageClock &ck : clocks)
+        for (int k = 0; k < FPO_NUM_STAGES; k++) ctx->stage_sec[k] += ck.sec[k];
 
     ctx->total_reads += R;
     ctx->filtered_reads += filtered;
@@ -1488,6 +1593,7 @@ int fpo_debug_last_batch(fpo_ctx *c, uint8_t *read_status, uint16_t *windows, in
 // single device's already reduced tables; build_read_group_table (device/read_group_table.cu:47-94);
 // compute_empirical_quality_scores (device/covariates.cu:314-340).
 int fpo_finalize(fpo_ctx *c) {
+    const double t_start = omp_get_wtime();
     ObsTable *obs[4] = {nullptr, &c->quality, &c->cycle, &c->context};
     const int qshift[4] = {2, 2, 12, 13};
     for (int t = 1; t < 4; t++) {
@@ -1543,7 +1649,12 @@ int fpo_finalize(fpo_ctx *c) {
             c->out_emp[t].push_back(r.empirical_quality);
         }
     }
+    c->stage_sec[FPO_STAGE_POSTPROCESS] += omp_get_wtime() - t_start;
     return 0;
+}
+
+void fpo_get_stage_seconds(const fpo_ctx *c, double out[FPO_NUM_STAGES]) {
+    for (int k = 0; k < FPO_NUM_STAGES; k++) out[k] = c->stage_sec[k];
 }
 
 int fpo_get_table(fpo_ctx *c, int32_t t, fp_table_view *out) {

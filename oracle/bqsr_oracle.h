@@ -36,6 +36,15 @@ void fpo_get_stats(const fpo_ctx *ctx, uint64_t out[4]);
 int fpo_debug_last_batch(fpo_ctx *ctx, uint8_t *read_status, uint16_t *windows, int16_t *hmm,
                          uint8_t *base_flags, uint8_t *baq_tag, double *frac_errors);
 
+/* Per-stage CPU time, in the categories the reference prints at exit (firepony.cu:195-223): thread-seconds
+ * summed over the OpenMP threads (the stages of one read run back to back on one thread). */
+enum {
+    FPO_STAGE_READ_FILTER = 0, FPO_STAGE_CIGAR_EXPANSION, FPO_STAGE_BP_FILTER, FPO_STAGE_SNP_FILTER,
+    FPO_STAGE_BAQ_SETUP, FPO_STAGE_BAQ_HMM, FPO_STAGE_BAQ_POST, FPO_STAGE_FRACTIONAL_ERROR,
+    FPO_STAGE_COVARIATES_GATHER, FPO_STAGE_COVARIATES_SORT_PACK, FPO_STAGE_POSTPROCESS, FPO_NUM_STAGES
+};
+void fpo_get_stage_seconds(const fpo_ctx *ctx, double out[FPO_NUM_STAGES]);
+
 /* Known-answer hooks for single functions. */
 /* BAQ HMM of one query against one reference window (device/baq.cu:214-697). ref/query are 4-bit symbols
  * one per byte. Outputs one quality and one state per query base. */

@@ -23,6 +23,10 @@ LIB = BUILD / "liboracle.so"
 
 _lib = None
 
+# FPO_STAGE_* order (bqsr_oracle.h)
+STAGES = ("read_filtering", "cigar_expansion", "bp_filtering", "snp_filtering", "baq_setup", "baq_hmm", "baq_post",
+          "fractional_error", "covariates_gather", "covariates_sort_pack", "post_processing")
+
 
 def build() -> Path:
     """Compiles the oracle (glibc libm, no fast-math, no FMA contraction, OpenMP over reads)."""
@@ -55,6 +59,7 @@ def lib():
                                   C.c_void_p, C.c_void_p]
         L.fpo_kat_empirical_quality.restype = C.c_double
         L.fpo_kat_empirical_quality.argtypes = [C.c_uint64, C.c_double, C.c_double, C.c_int]
+        L.fpo_get_stage_seconds.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.fpo_kat_baq_quality_from_max.restype = C.c_int
         L.fpo_kat_baq_quality_from_max.argtypes = [C.c_double]
         _lib = L
@@ -101,6 +106,13 @@ class Oracle:
         a = (C.c_uint64 * 4)()
         lib().fpo_get_stats(self.h, a)
         return {"total_reads": a[0], "filtered_reads": a[1], "baq_reads": a[2], "num_batches": a[3]}
+
+    def stage_seconds(self) -> dict:
+        """CPU thread-seconds per stage since creation, in the reference's exit-statistics categories
+        (firepony.cu:195-223)."""
+        a = (C.c_double * len(STAGES))()
+        lib().fpo_get_stage_seconds(self.h, a)
+        return {name: a[i] for i, name in enumerate(STAGES)}
 
     def debug_last_batch(self, batch) -> dict:
         R, Q = batch.num_reads, batch.num_qualities

@@ -25,3 +25,22 @@ def test_failing_leg_is_reported_not_raised():
     out = bench._leg(boom, "gpu")
     assert out == {"error": "RuntimeError: no gpu"}
     assert bench._leg(lambda a, b: a + b, 2, 3) == 5
+
+
+def test_cpu_baseline_times_the_oracle_on_prebuilt_ranges():
+    """The CPU leg's 1000-read sub-batches are zero-copy ranges that cover the batch in order, and the leg
+    reports the per-stage CPU breakdown in the reference's exit-statistics categories."""
+    import numpy as np
+    import bench
+    from oracle.oracle import STAGES
+    from tests.conftest import make_dataset
+    p, ref, batches = make_dataset("precision_20M_151bp_pe", 2500, 2500, 300_000)
+    subs = bench.cpu_sub_batches(batches[0])
+    assert [s.num_reads for s in subs] == [1000, 1000, 500]
+    # views, not copies: the qualities of the second range are the batch's own memory
+    assert np.shares_memory(subs[1]["qualities"], batches[0]["qualities"])
+    out = bench.cpu_baseline(ref, batches, 0.2)
+    assert out["value"] > 0 and out["kind"] == "port"
+    assert set(out["stages"]["share"]) == set(STAGES)
+    assert abs(sum(out["stages"]["share"].values()) - 1.0) < 1e-3
+    assert out["stages"]["thread_s"]["baq_hmm"] > 0

@@ -43,6 +43,20 @@ def test_bam_library_exports_every_declared_symbol(native):
     assert not missing, f"missing exports: {missing}"
 
 
+def test_sort_entries_rejects_sizes_beyond_32_bit_offsets(native):
+    """fp_sort_entries refuses n above FP_SORT_MAX_ENTRIES before it touches the device (its digit counts and
+    offsets are 32-bit), and fp_sort_entries_static refuses n above its fixed scratch."""
+    from firepony_gb300.abi import FP_BAD_INPUT
+    from firepony_gb300.engine import lib
+    L = lib()
+    assert L.fp_sort_entries(16, 32, (1 << 32) - 1, 29, None) == FP_BAD_INPUT
+    assert L.fp_sort_entries(16, 32, 1 << 33, 29, None) == FP_BAD_INPUT
+    assert L.fp_sort_entries(16, 32, 100, 33, None) == FP_BAD_INPUT
+    assert L.fp_sort_entries_static(16, 32, (1 << 20) + 1, 29, None) == FP_BAD_INPUT
+    text = (ROOT / "include" / "firepony_gb300.h").read_text()
+    assert re.search(r"#define FP_SORT_MAX_ENTRIES 0xFFFFFFFEull", text)
+
+
 def test_report_format_small_table(native, tmp_path):
     from firepony_gb300.engine import write_report
     t = {}
@@ -87,7 +101,10 @@ def test_synth_batches_are_consistent_and_deterministic():
     assert set(np.unique(b["read_len"])) <= {36, 76, 101, 151, 250}
 
 
-def test_oracle_independent_of_threads_and_batching():
+@pytest.mark.parametrize("threads", [4, 7])
+def test_oracle_independent_of_threads_and_batching(threads):
+    """The oracle's parallel sort/merge/fold (chunk runs merged pairwise, the running table merged in key
+    ranges) gives the tables of one sequential pass, for any thread count and batch size."""
     from oracle.oracle import Oracle
     p, ref, batches = make_dataset("precision_20M_151bp_pe", 3000, 3000, 300_000)
     whole = batches[0]
@@ -98,7 +115,7 @@ def test_oracle_independent_of_threads_and_batching():
     o2 = Oracle(p.num_read_groups)
     o2.load_reference(ref)
     for i in range(0, whole.num_reads, 700):
-        o2.process(whole.subset(np.arange(i, min(i + 700, whole.num_reads))), threads=4)
+        o2.process(whole.range(i, min(i + 700, whole.num_reads)), threads=threads)
     t2 = o2.finalize()
     for t in range(4):
         for k in t1[t]:

@@ -47,3 +47,22 @@ def test_sort_entries_skewed_digits(native):
     sort_entries(d_in.data_ptr(), d_out.data_ptr(), n, 29)
     torch.cuda.synchronize()
     np.testing.assert_array_equal(d_out.cpu().numpy().view(np.uint64), reference_sort(a, 29))
+
+
+@pytest.mark.parametrize("key_bits", [20, 13])
+def test_sort_entries_ignores_bits_above_key_bits(native, key_bits):
+    """Only key bits below key_bits decide the order: entries whose keys differ only above it (the last
+    digit of a width that is not a multiple of the digit size) keep their input order."""
+    import torch
+    from firepony_gb300.engine import sort_entries
+    rng = np.random.default_rng(key_bits)
+    n = 300_001
+    low = rng.integers(0, 1 << key_bits, n, dtype=np.uint64)
+    high = rng.integers(0, 1 << (32 - key_bits), n, dtype=np.uint64) << np.uint64(key_bits)  # noise above key_bits
+    payload = np.arange(n, dtype=np.uint64)
+    a = ((low | high) << np.uint64(32)) | payload
+    d_in = torch.from_numpy(a.view(np.int64).copy()).cuda()
+    d_out = torch.empty_like(d_in)
+    sort_entries(d_in.data_ptr(), d_out.data_ptr(), n, key_bits)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(d_out.cpu().numpy().view(np.uint64), reference_sort(a, key_bits))
