@@ -48,16 +48,24 @@ def parse():
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--replay-rpw", type=int, default=0, help="reads per warp of the FP64 replay kernels (0: default)")
-    ap.add_argument("--plain-steps", type=int, default=2, help="batches through the plain FP64 path (0: skip)")
+    ap.add_argument("--plain-steps", type=int, default=-1,
+                    help="batches through the plain FP64 path, tables compared with the timed run (-1: all, 0: skip)")
+    ap.add_argument("--no-precision", action="store_true", help="skip the FP32 vs FP64 per-read precision trace")
     ap.add_argument("--engine-flags", type=int, default=0, help="fp_options.flags (FP_FLAG_*) for the timed engine")
     ap.add_argument("--bam-batches", type=int, default=8, help="workload batches for the BAM input measurement (0: skip)")
-    ap.add_argument("--config-legs", action="store_true",
-                    help="also measure the plain 100k-read configuration and the large single run")
-    ap.add_argument("--large-batches", type=int, default=5, help="2M-read batches of the large single run")
-    ap.add_argument("--batched-batches", type=int, default=96,
+    ap.add_argument("--no-config-legs", action="store_true",
+                    help="skip the plain 100k-read configuration and the large single run")
+    ap.add_argument("--large-reads", type=int, default=100_000_000, help="reads of the large single run")
+    ap.add_argument("--large-batch-reads", type=int, default=2_000_000, help="batch size of the large single run")
+    ap.add_argument("--large-fp64-batches", type=int, default=3,
+                    help="batches of the large run also run through the plain FP64 path (tables compared)")
+    ap.add_argument("--batched-batches", type=int, default=4096,
                     help="input batches of the uneven-batch measurement (0: skip)")
-    ap.add_argument("--coalesce-reads", type=int, default=1_000_000, help="fp_options.coalesce_reads of its coalesced run")
-    ap.add_argument("--serve-jobs", type=int, default=128, help="jobs of the serving measurement (0: skip)")
+    ap.add_argument("--batched-sample", type=int, default=96,
+                    help="batches of its per-batch / plain FP64 comparison runs")
+    ap.add_argument("--coalesce-reads", type=int, default=1_000_000, help="fp_options.coalesce_reads of the sample's coalesced run")
+    ap.add_argument("--no-autotune", action="store_true", help="run the uneven batches with the default shapes")
+    ap.add_argument("--serve-jobs", type=int, default=256, help="jobs of the serving measurement (0: skip)")
     ap.add_argument("--no-refstore", action="store_true", help="skip the reference store start-up measurement")
     ap.add_argument("--sort-entries", type=int, default=64_000_000, help="entries of the radix sort measurement (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="job arrivals per second (Poisson)")
@@ -120,17 +128,23 @@ def make_workload(num_batches, batch_reads):
     return p, ref, batches
 
 
+def tables_identical(a: dict, b: dict) -> bool:
+    import numpy as np
+    return all(np.array_equal(a[t][k], b[t][k]) for t in a for k in a[t])
+
+
 def run_plain(args, res):
-    """The plain path (every BAQ read in exact FP64, FP_BAQ_FP64) on the first batches of the same workload,
-    inputs resident in HBM, CUDA events on the engine's stream."""
+    """The plain path (every BAQ read in exact FP64, FP_BAQ_FP64) on the same device-resident batches as the
+    timed run (all of them by default), CUDA events on the engine's stream; its tables are compared with the
+    timed FP32 run's."""
     import torch
     from firepony_gb300.engine import Engine
-    n = min(args.plain_steps, len(res["batches"]))
+    n = len(res["dev"]) if args.plain_steps < 0 else min(args.plain_steps, len(res["dev"]))
     p = res["ref"].preset
     eng = Engine(num_read_groups=p.num_read_groups, baq_mode="fp64")
     eng.load_reference(res["ref"])
     stream = torch.cuda.ExternalStream(eng.stream)
-    dev = [to_device(b) for b in res["batches"][:n]]
+    dev = res["dev"][:n]
     eng.submit_device_view(dev[0][1])  # warm-up
     eng.finalize()
     eng.reset()
@@ -139,101 +153,244 @@ def run_plain(args, res):
     e0.record(stream)
     for _, v in dev:
         eng.submit_device_view(v)
-    eng.finalize()
+    tables = eng.finalize()
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     eng.close()
     reads = n * args.batch_reads
-    return {"value": reads / (ms / 1e3), "unit": "reads/s", "baq": "fp64 (every BAQ read exact FP64)",
-            "steps": n, "ms_per_step": ms / n}
+    out = {"value": reads / (ms / 1e3), "unit": "reads/s", "baq": "fp64 (every BAQ read exact FP64)",
+           "steps": n, "ms_per_step": ms / n}
+    if n == len(res["dev"]):
+        out["fp32_fp64_tables_identical"] = tables_identical(tables, res["tables"])
+        out["compared"] = f"all four tables of the timed FP32 job ({reads} reads) against this FP64 job"
+    return out
+
+
+def run_precision(args, res):
+    """FP32 vs FP64 error per read on the timed job's batches: an FP32 engine with the precision trace
+    (FP_FLAG_PRECISION_TRACE) also runs every BAQ read through the plain FP64 HMM and compares the pre-floor
+    MAP quality t = -4.343 ln(1 - p_max) + 0.499 base by base (bases with FP64 t below 101; above it every
+    capped quality is 99). Per read: the largest |t32 - t64| and the widest certified half-interval, as
+    percentiles over reads; bound violations count bases whose FP64 t lies outside the FP32 interval."""
+    from firepony_gb300.abi import FP_FLAG_PRECISION_TRACE, precision_percentile
+    from firepony_gb300.engine import Engine
+    p = res["ref"].preset
+    eng = Engine(num_read_groups=p.num_read_groups, baq_mode="fp32", flags=FP_FLAG_PRECISION_TRACE)
+    eng.load_reference(res["ref"])
+    for _, v in res["dev"]:
+        eng.submit_device_view(v)
+    tables = eng.finalize()
+    ps = eng.precision_stats()
+    st = eng.stats()
+    eng.close()
+    qs = (0.5, 0.9, 0.99, 0.999, 1.0)
+    return {"reads_compared": ps["reads"], "reads_without_fp32_values": ps["reads_without_fp32"],
+            "bases_compared": ps["bases"], "bound_violations": ps["bound_violations"],
+            "max_abs_error": ps["max_abs_error"], "max_certified_half_width": ps["max_half_width"],
+            "per_read_max_abs_error_upper_edge": {f"p{q * 100:g}": precision_percentile(ps["err_hist"], q) for q in qs},
+            "per_read_certified_half_width_upper_edge": {f"p{q * 100:g}": precision_percentile(ps["width_hist"], q)
+                                                         for q in qs},
+            "err_hist": ps["err_hist"], "width_hist": ps["width_hist"],
+            "hist_bins": "bin 0 = exactly 0; bin 1+k = [10^(-10+k/4), 10^(-10+(k+1)/4)); bin 41 = >= 1",
+            "baq_reads": st["baq_reads"], "escalated_to_fp64": st["baq_fp64_escalated_reads"],
+            "escalated_fraction": st["baq_fp64_escalated_reads"] / max(1, st["baq_reads"]),
+            "tables_identical_to_timed_run": tables_identical(tables, res["tables"]),
+            "quantity": "t = -4.343 ln(1 - p_max) + 0.499 before flooring (device/baq.cu:673), per base"}
+
+
+def generate_into(ref, sizes, sink, first_index=0):
+    """Generates batch i (i = 0..len(sizes)-1, batch index first_index + i) on host threads and hands each to
+    sink(i, batch) in order; generated batches not yet handed over are bounded by the pool's width."""
+    from concurrent.futures import ThreadPoolExecutor
+    workers = min(16, os.cpu_count() or 4)
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        pending = {}
+        nxt = 0
+        for i in range(len(sizes)):
+            while len(pending) < 2 * workers and nxt < len(sizes):
+                pending[nxt] = ex.submit(ref.batch, first_index + nxt, int(sizes[nxt]))
+                nxt += 1
+            sink(i, pending.pop(i).result())
 
 
 def run_batched(args):
     """The uneven-batch workload (4 contigs / 100 Mbp, reads of 36-250 bp mixed, 0-8 indels per read, 10% wide
-    deletions, 16 read groups) as a bounded sample of its many small input batches (sizes uniform in 2k-40k
-    reads), from page-locked host buffers through the C ABI: each batch processed alone, then with the engine
-    coalescing them (fp_options.coalesce_reads) into device batches, and the plain FP64 path on the same
-    coalesced batches. Wall clock from the first submit to the finished tables; all runs must give identical
-    tables."""
-    import numpy as np
+    deletions, 16 read groups) as its 4,096 input batches of 2k-40k reads, from page-locked host buffers
+    through the C ABI. The autotuner picks the engine's runtime shapes (FP64 replay layout, device batch size)
+    on a separate 16-batch sample; the whole workload then runs with them (wall clock from the first submit to
+    the finished tables). On a bounded sample of the same batches: each batch processed alone, the engine
+    coalescing them into device batches, and the plain FP64 path on the coalesced batches, which must all give
+    identical tables."""
     from firepony_gb300 import synth
-    from firepony_gb300.engine import Engine, PinnedBatch
+    from firepony_gb300.autotune import autotune
+    from firepony_gb300.engine import Engine, PinnedPool
     sizes = synth.uneven_batch_sizes(args.batched_batches, 2000, 40000, seed=2)
     p = synth.PRESETS["batched_uneven"].scaled(num_reads=int(sizes.sum()))
     ref = synth.Reference(p)
-    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
-        batches = list(ex.map(lambda i: ref.batch(i, int(sizes[i])), range(len(sizes))))
-    pinned = [PinnedBatch(b) for b in batches]
-    reads = int(sizes.sum())
     out = {}
-    tables = {}
-    # the plain path (every BAQ read in exact FP64) on the same coalesced device batches
-    for name, coalesce, mode in (("per_batch", 0, "fp32"), ("coalesced", args.coalesce_reads, "fp32"),
-                                 ("plain_fp64_coalesced", args.coalesce_reads, "fp64")):
-        eng = Engine(num_read_groups=p.num_read_groups, coalesce_reads=coalesce, baq_mode=mode)
+    best = {"replay_reads_per_warp": 0, "coalesce_reads": args.coalesce_reads}
+    if not args.no_autotune:
+        tsz = synth.uneven_batch_sizes(16, 2000, 40000, seed=5)
+        tune = [ref.batch(1_000_000 + i, int(n)) for i, n in enumerate(tsz)]  # batches not in the workload
+        t0 = time.perf_counter()
+        tuned = autotune(ref, tune, p.num_read_groups)
+        best = tuned["best"]
+        out["autotune"] = {"sample_reads": tuned["reads"], "best": best, "seconds": time.perf_counter() - t0,
+                           "candidates": len(tuned["results"])}
+    pool = PinnedPool()
+    pinned = [None] * len(sizes)
+    t0 = time.perf_counter()
+    generate_into(ref, sizes, lambda i, b: pinned.__setitem__(i, pool.add(b)))
+    out["generate_s"] = time.perf_counter() - t0
+    reads = int(sizes.sum())
+    try:
+        # the whole workload with the tuned shapes
+        eng = Engine(num_read_groups=p.num_read_groups, coalesce_reads=best["coalesce_reads"],
+                     replay_reads_per_warp=best["replay_reads_per_warp"])
         eng.load_reference(ref)
-        # warm-up: one untimed pass over the same batches (device buffers grown to the job's largest batch)
-        eng.submit_pipelined([pb.batch for pb in pinned])
+        eng.submit_pipelined(pinned[:64])  # warm-up (device buffers grown), not timed
         eng.finalize()
         eng.reset()
         t0 = time.perf_counter()
-        # (per batch: each batch's copy is prefetched while the previous one runs; coalesced: copied at submit)
-        eng.submit_pipelined([pb.batch for pb in pinned])
-        tables[name] = eng.finalize()
+        eng.submit_pipelined(pinned)
+        eng.finalize()
         dt = time.perf_counter() - t0
-        out[name + "_reads_per_s"] = reads / dt
+        st = eng.stats()
         eng.close()
-    same = all(np.array_equal(tables["per_batch"][t][k], tables[other][t][k])
-               for other in ("coalesced", "plain_fp64_coalesced") for t in tables["per_batch"] for k in tables["per_batch"][t])
-    if not args.no_cpu_baseline:
-        out["cpu_oracle"] = cpu_baseline(ref, batches, args.cpu_sample_seconds / 3)
+        out["reads_per_s"] = reads / dt
+        out["seconds"] = dt
+        out["stage_ms"] = [round(x, 2) for x in st["gpu_ms_per_stage"]]
+        out["device_batches"] = st["num_batches"]
+        out["baq_reads_by_band"] = st["baq_reads_by_band"]
+        out["baq_escalated_by_band"] = st["baq_escalated_by_band"]
+        out["baq_fp64_escalated_reads"] = st["baq_fp64_escalated_reads"]
+        # bounded sample: per batch / coalesced / plain FP64 coalesced, identical tables
+        sample = pinned[:args.batched_sample]
+        sreads = int(sum(b.num_reads for b in sample))
+        tables = {}
+        for name, coalesce, mode in (("per_batch", 0, "fp32"), ("coalesced", args.coalesce_reads, "fp32"),
+                                     ("plain_fp64_coalesced", args.coalesce_reads, "fp64")):
+            eng = Engine(num_read_groups=p.num_read_groups, coalesce_reads=coalesce, baq_mode=mode)
+            eng.load_reference(ref)
+            eng.submit_pipelined(sample)  # warm-up pass over the same batches
+            eng.finalize()
+            eng.reset()
+            t0 = time.perf_counter()
+            eng.submit_pipelined(sample)
+            tables[name] = eng.finalize()
+            out["sample_" + name + "_reads_per_s"] = sreads / (time.perf_counter() - t0)
+            eng.close()
+        out["sample_tables_identical"] = all(tables_identical(tables["per_batch"], tables[o])
+                                             for o in ("coalesced", "plain_fp64_coalesced"))
+        out["sample"] = f"first {len(sample)} batches, {sreads} reads"
+        if not args.no_cpu_baseline:
+            out["cpu_oracle"] = cpu_baseline(ref, [pinned[0]], args.cpu_sample_seconds / 3)
+    finally:
+        del pinned
+        pool.close()
     return {"workload": "batched_uneven: 4 contigs / 100 Mbp, reads of 36/76/101/151/250 bp, 0-8 indels per read, "
                         "10% wide deletions, 16 read groups",
-            "batches": len(sizes), "reads": reads, "batch_reads": "uniform 2000-40000", "coalesce_reads": args.coalesce_reads,
-            **out, "speedup": out["coalesced_reads_per_s"] / out["per_batch_reads_per_s"],
-            "vs_plain_fp64": out["coalesced_reads_per_s"] / out["plain_fp64_coalesced_reads_per_s"],
-            "tables_identical": bool(same),
+            "batches": len(sizes), "reads": reads, "batch_reads": "uniform 2000-40000", "tuned_shapes": best,
+            **out,
+            "vs_sample_per_batch": out["reads_per_s"] / out["sample_per_batch_reads_per_s"],
+            "sample_vs_plain_fp64": out["sample_coalesced_reads_per_s"] / out["sample_plain_fp64_coalesced_reads_per_s"],
             "inputs": "page-locked host buffers through fp_engine_submit_batch (copies in the timed region)"}
 
 
 def run_config_legs(args):
-    """The plain configuration (1 Mbp contig, 100k single-end 101 bp reads, one read group) and the large single
-    run (3 contigs / 250 Mbp, 151 bp pairs, 32 read groups, 5% duplicates and 1% unmapped reads filtered, 3.3M
-    known sites) through the C ABI from page-locked host buffers, FP32 and plain FP64, with the CPU oracle on a
-    bounded sample of each. The large run streams `--large-batches` 2M-read batches of its 100M-read workload
-    into one resident set of tables (the reads processed are stated)."""
-    import numpy as np
+    """The plain configuration (1 Mbp contig, 100k single-end 101 bp reads, one read group) from page-locked host
+    buffers through the C ABI, FP32 and plain FP64; and the large single run (3 contigs / 250 Mbp, 151 bp pairs,
+    32 read groups, 5% duplicates and 1% unmapped or MAPQ-0 reads filtered, 3.3M known sites) at its full 100M
+    reads: batches generated on host threads and moved to HBM as they come, then one job over all of them
+    with the inputs resident (CUDA events on the engine's stream), the full covariate tables resident and
+    folded batch by batch. Its first batches also run through the plain FP64 path and an FP32 engine, whose
+    tables must be equal. The CPU oracle runs on a bounded sample of each."""
+    import torch
     from firepony_gb300 import synth
     from firepony_gb300.engine import Engine, PinnedBatch
     out = {}
-    for name, preset, nb, per in (("plain_100k_101bp", "plain_100k_101bp", 1, 100_000),
-                                  ("large_100M_151bp_pe", "large_100M_151bp_pe", args.large_batches, 2_000_000)):
-        p = synth.PRESETS[preset]
-        ref = synth.Reference(p)
-        with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
-            batches = list(ex.map(lambda i: ref.batch(i, per), range(nb)))
-        pinned = [PinnedBatch(b) for b in batches]
-        reads = nb * per
-        row = {"reads": reads}
-        tables = {}
-        for mode in ("fp32", "fp64"):
-            eng = Engine(num_read_groups=p.num_read_groups, baq_mode=mode)
-            eng.load_reference(ref)
-            eng.submit_pipelined([pinned[0].batch])  # warm-up
-            eng.finalize()
-            eng.reset()
-            t0 = time.perf_counter()
-            eng.submit_pipelined([pb.batch for pb in pinned])
-            tables[mode] = eng.finalize()
-            row[mode + "_reads_per_s"] = reads / (time.perf_counter() - t0)
-            eng.close()
-        row["fp32_fp64_tables_identical"] = all(np.array_equal(tables["fp32"][t][k], tables["fp64"][t][k])
-                                                for t in tables["fp32"] for k in tables["fp32"][t])
-        row["cpu_oracle"] = cpu_baseline(ref, batches, args.cpu_sample_seconds / 3)
-        for pb in pinned:
-            pb.close()
-        out[name] = row
+    # plain configuration
+    p = synth.PRESETS["plain_100k_101bp"]
+    ref = synth.Reference(p)
+    b0 = ref.batch(0, 100_000)
+    pb = PinnedBatch(b0)
+    row = {"reads": 100_000}
+    tables = {}
+    for mode in ("fp32", "fp64"):
+        eng = Engine(num_read_groups=p.num_read_groups, baq_mode=mode)
+        eng.load_reference(ref)
+        eng.submit_pipelined([pb.batch])  # warm-up
+        eng.finalize()
+        eng.reset()
+        t0 = time.perf_counter()
+        eng.submit_pipelined([pb.batch])
+        tables[mode] = eng.finalize()
+        row[mode + "_reads_per_s"] = 100_000 / (time.perf_counter() - t0)
+        eng.close()
+    pb.close()
+    row["fp32_fp64_tables_identical"] = tables_identical(tables["fp32"], tables["fp64"])
+    if not args.no_cpu_baseline:
+        row["cpu_oracle"] = cpu_baseline(ref, [b0], args.cpu_sample_seconds / 3)
+    out["plain_100k_101bp"] = row
+    # large single run
+    p = synth.PRESETS["large_100M_151bp_pe"]
+    ref = synth.Reference(p)
+    per = args.large_batch_reads
+    nb = (args.large_reads + per - 1) // per
+    sizes = [min(per, args.large_reads - i * per) for i in range(nb)]
+    dev = [None] * nb
+    first = {}
+
+    def sink(i, b):
+        dev[i] = to_device(b)
+        if i == 0:
+            first["batch"] = b
+    t0 = time.perf_counter()
+    generate_into(ref, sizes, sink)
+    row = {"reads": int(sum(sizes)), "batches": nb, "batch_reads": per, "generate_and_upload_s": time.perf_counter() - t0}
+    try:
+        eng = Engine(num_read_groups=p.num_read_groups)
+        eng.load_reference(ref)
+        stream = torch.cuda.ExternalStream(eng.stream)
+        eng.submit_device_view(dev[0][1])  # warm-up
+        eng.finalize()
+        eng.reset()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _, v in dev:
+            eng.submit_device_view(v)
+        eng.finalize()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        st = eng.stats()
+        eng.close()
+        row["fp32_reads_per_s"] = row["reads"] / (ms / 1e3)
+        row["ms_per_batch"] = ms / nb
+        row["filtered_reads"] = st["filtered_reads"]
+        row["baq_fp64_escalated_reads"] = st["baq_fp64_escalated_reads"]
+        k = min(args.large_fp64_batches, nb)
+        if k:
+            tabs = {}
+            for mode in ("fp32", "fp64"):
+                eng = Engine(num_read_groups=p.num_read_groups, baq_mode=mode)
+                eng.load_reference(ref)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                for _, v in dev[:k]:
+                    eng.submit_device_view(v)
+                tabs[mode] = eng.finalize()
+                row[f"first_{k}_batches_{mode}_reads_per_s"] = sum(sizes[:k]) / (time.perf_counter() - t0)
+                eng.close()
+            row[f"first_{k}_batches_fp32_fp64_tables_identical"] = tables_identical(tabs["fp32"], tabs["fp64"])
+        if not args.no_cpu_baseline:
+            row["cpu_oracle"] = cpu_baseline(ref, [first["batch"]], args.cpu_sample_seconds / 3)
+    finally:
+        del dev
+        torch.cuda.empty_cache()
+    out["large_100M_151bp_pe"] = row
     return out
 
 
@@ -545,8 +702,6 @@ def run_gb300(args, rank, world):
     ms_value = e0.elapsed_time(e1)
     st = eng.stats()
     launches = st["gpu_kernel_launches"] - launches0
-    del dev
-    torch.cuda.empty_cache()
 
     # ---- e2e: pinned host buffers through the C ABI ----
     eng.reset()
@@ -572,10 +727,26 @@ def run_gb300(args, rank, world):
     stage_ms = st["gpu_ms_per_stage"]
     eng.close()
     return dict(ms_value=ms_value, t_e2e=t_e2e, reads=K * args.batch_reads, h2d=h2d, d2h=d2h, launches=launches,
-                clocks=clk, stats=st, stage_ms=stage_ms, same=same, ref=ref, batches=batches)
+                clocks=clk, stats=st, stage_ms=stage_ms, same=same, ref=ref, batches=batches, dev=dev, tables=tables)
 
 
-def roofline(res, args):
+def fp32_peak():
+    """The FP32 SIMT roofline denominator: measured on this GPU (fp_measure_fp32_peak: scalar and packed
+    multiply-add chains over one resident grid), beside the nominal SMs x 128 lanes x 2 flops x max clock
+    from the device's own SM count."""
+    import torch
+    from firepony_gb300.engine import measure_fp32_peak
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    out = {"sms": props.multi_processor_count}
+    try:
+        out["scalar_fma_tflops"] = measure_fp32_peak(torch.cuda.current_device(), packed=False)
+        out["packed_fma2_tflops"] = measure_fp32_peak(torch.cuda.current_device(), packed=True)
+    except Exception as ex:  # noqa: BLE001 - reported, the nominal figure stays
+        out["error"] = str(ex)
+    return out
+
+
+def roofline(res, args, peak32):
     """Roofline of the dominant kernel, the band-class-0 BAQ HMM (k_baq_tpr<float, 15>: bandwidth 7, FP32 with
     certified bounds), timed by the engine with CUDA events around each of its launches inside the timed
     region. Algorithmic bytes per read of that class (L = mean HMM query length): L/2 packed bases + L
@@ -600,17 +771,20 @@ def roofline(res, args):
     bytes_ = reads * (L / 2 + L + (L + 6) / 2 + L + 4 * L)
     achieved_gbs = bytes_ / (ms / 1e3) / 1e9
     tops = cells * 41 / (ms / 1e3) / 1e12
-    sm_mhz = res["clocks"].get("sm_max_mhz") or 2070.0
-    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    sm_mhz = res["clocks"].get("sm_max_mhz") or peaks.get("sm_max_mhz") or 2070.0
+    nominal = peak32["sms"] * 128 * 2 * sm_mhz * 1e6 / 1e12
+    measured = max(peak32.get("scalar_fma_tflops", 0.0), peak32.get("packed_fma2_tflops", 0.0))
+    f32 = measured if measured > 0 else nominal
     return {"bound": "hbm", "achieved": round(achieved_gbs, 2), "peak": hbm, "unit": "GB/s",
             "frac": round(achieved_gbs / hbm, 5), "traffic": TRAFFIC_BYTES_PER_LAUNCH,
             "kernel": "k_baq_tpr<float,15> (BAQ HMM, band class 0)",
             "launch_ms": round(ms, 3), "reads_per_launch": int(reads), "band_cells_per_launch": int(cells),
             "peak_source": "measured" if peaks else "fallback",
-            "compute": {"unit": "TFLOP/s", "achieved": round(tops, 3), "peak": round(fp32_peak, 1),
-                        "peak_source": "nominal FP32 SIMT (152 SMs x 128 lanes x FMA x max SM clock)",
-                        "frac": round(tops / fp32_peak, 4),
-                        "note": "binding roofline: FP32 SIMT issue; forward rows spill to HBM scratch"}}
+            "compute": {"unit": "TFLOP/s", "achieved": round(tops, 3), "peak": round(f32, 2),
+                        "peak_source": "measured" if measured > 0 else "nominal",
+                        "peak_measured": peak32, "peak_nominal": round(nominal, 2),
+                        "frac": round(tops / f32, 4),
+                        "note": "binding roofline: FP32 SIMT issue"}}
 
 
 def _leg(fn, *a):
@@ -676,11 +850,19 @@ def main():
         cpu = None
         if not args.no_cpu_baseline and world == 1:
             cpu = _leg(cpu_baseline, res["ref"], res["batches"], args.cpu_sample_seconds)
-        plain = _leg(run_plain, args, res) if args.plain_steps > 0 and world == 1 and args.baq == "fp32" else None
+        plain = _leg(run_plain, args, res) if args.plain_steps != 0 and world == 1 and args.baq == "fp32" else None
+        precision = (_leg(run_precision, args, res) if not args.no_precision and world == 1 and args.baq == "fp32"
+                     else None)
+        res["dev"] = None  # the device-resident batches of the timed job are not needed past this point
+        import torch
+        torch.cuda.empty_cache()
+        peak32 = _leg(fp32_peak) if world == 1 else {"sms": torch.cuda.get_device_properties(0).multi_processor_count}
+        if "sms" not in peak32:
+            peak32["sms"] = torch.cuda.get_device_properties(0).multi_processor_count
         serving = _leg(run_serving, args) if args.serve_jobs > 0 and world == 1 else None
         bam_in = _leg(run_bam, args, res) if args.bam_batches > 0 and world == 1 else None
         batched = _leg(run_batched, args) if args.batched_batches > 0 and world == 1 else None
-        configs = _leg(run_config_legs, args) if args.config_legs and world == 1 else None
+        configs = _leg(run_config_legs, args) if not args.no_config_legs and world == 1 else None
         refstore = _leg(run_refstore, args) if not args.no_refstore and world == 1 else None
         sort = _leg(run_sort, args) if args.sort_entries > 0 and world == 1 else None
         line = {"metric": METRIC, "value": value, "unit": "reads/s", "n_gpus": world, "steps": args.steps,
@@ -692,9 +874,10 @@ def main():
                 "e2e": {"value": e2e, "unit": "reads/s", "h2d_bytes_per_step": int(res["h2d"]),
                         "d2h_bytes_per_step": int(res["d2h"])},
                 "gpu_launches": res["launches"],
-                "roofline": roofline(res, args),
+                "roofline": roofline(res, args, peak32),
                 "cpu_baseline": cpu,
                 "plain": plain,
+                "precision": precision,
                 "serving": serving,
                 "bam": bam_in,
                 "batched": batched,

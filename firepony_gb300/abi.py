@@ -17,6 +17,7 @@ class FpOptions(C.Structure):
                 ("max_batch_cigar_ops", C.c_uint64), ("replay_reads_per_warp", C.c_uint32),
                 ("flags", C.c_uint32), ("coalesce_reads", C.c_uint32), ("reserved", C.c_uint32)]
 FP_FLAG_REPLAY_ALL = 1
+FP_FLAG_PRECISION_TRACE = 2
 
 
 class FpBatchView(C.Structure):
@@ -46,6 +47,31 @@ class FpStats(C.Structure):
                 ("baq_escalated_by_cause", C.c_uint64 * 2),
                 ("baq_band_cells", C.c_uint64 * 3), ("baq_main_launches", C.c_uint64),
                 ("baq_main_ms", C.c_double), ("baq_path_ms", C.c_double * 4)]
+
+
+class FpPrecisionStats(C.Structure):
+    _fields_ = [("reads", C.c_uint64), ("reads_without_fp32", C.c_uint64), ("bases", C.c_uint64),
+                ("bound_violations", C.c_uint64), ("max_abs_error", C.c_double), ("max_half_width", C.c_double),
+                ("err_hist", C.c_uint64 * 42), ("width_hist", C.c_uint64 * 42)]
+
+
+# lower edge of precision-histogram bin i (bin 0 holds exactly 0; bin 1 + k starts at 10^(-10 + k/4))
+def precision_bin_lower(i: int) -> float:
+    return 0.0 if i == 0 else 10.0 ** (-10.0 + (i - 1) / 4.0)
+
+
+def precision_percentile(hist, q: float) -> float:
+    """Upper edge of the histogram bin that holds the q-quantile (0 < q <= 1) of the per-read values."""
+    total = sum(hist)
+    if not total:
+        return 0.0
+    need = q * total
+    acc = 0
+    for i, c in enumerate(hist):
+        acc += c
+        if acc >= need:
+            return 0.0 if i == 0 else (float("inf") if i == len(hist) - 1 else precision_bin_lower(i + 1))
+    return float("inf")
 
 
 class FpRefstoreInfo(C.Structure):

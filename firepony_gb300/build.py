@@ -35,6 +35,8 @@ ENGINE_UNITS = [
     ("k_covariates.cu", []),
     ("k_sort.cu", []),
     ("k_post.cu", ["-fmad=false"]),    # empirical quality: exact IEEE double sums and products
+    ("k_precision.cu", []),             # precision trace: FP32 vs FP64 MAP quality per read
+    ("k_probe.cu", []),                 # FP32 SIMT throughput probe (roofline denominator)
     ("report.cpp", []),
     ("refstore.cu", []),                # reference store: shared-memory segments, one device copy per GPU
 ]

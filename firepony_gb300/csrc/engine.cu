@@ -128,6 +128,7 @@ struct fp_engine {
     DevBatch batch{};
     DevBuf oplen, cigoff, ev_rc, ev_type, per_read, per_base, lists, counters, entry_cnt, entry_off;
     DevBuf entries, entries_alt, sort_tmp, scan_tmp, s32, s32b, s64, s32w;  // s32w: wide-band exact FP64 scratch
+    DevBuf trace32, trace64, prec_acc;  // precision trace (FP_FLAG_PRECISION_TRACE)
     u64 s64_doubles = 0;
     BatchWork work{};
     uint32_t last_R = 0;
@@ -663,6 +664,23 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
     w.entry_count = eng->entry_cnt.as<u32>();
     w.entry_offset = eng->entry_off.as<u32>();
     CK(cudaMemsetAsync(w.tag, 0xFF, Q, st), "tag init");
+    // precision trace: the FP32 kernels record t and its interval per base; the plain FP64 path is run on
+    // the same reads after the BAQ stage (FP32 mode only)
+    const bool trace = (eng->flags & FP_FLAG_PRECISION_TRACE) && eng->baq_mode == FP_BAQ_FP32;
+    w.trace32 = nullptr;
+    w.trace64 = nullptr;
+    if (trace) {
+        CK(eng->trace32.ensure(al(Q * 12 + 12)), "precision trace");
+        CK(eng->trace64.ensure(al(Q * 8 + 8)), "precision trace");
+        if (!eng->prec_acc.p) {
+            CK(eng->prec_acc.ensure(sizeof(PrecisionAcc)), "precision trace");
+            CK(cudaMemsetAsync(eng->prec_acc.p, 0, sizeof(PrecisionAcc), st), "precision trace");
+        }
+        w.trace32 = eng->trace32.as<float>();
+        w.trace64 = eng->trace64.as<double>();
+        CK(cudaMemsetAsync(w.trace32, 0xFF, Q * 12, st), "precision trace");  // NaN: no FP32 value
+        CK(cudaMemsetAsync(w.trace64, 0, Q * 8, st), "precision trace");
+    }
     cudaEventRecord(eng->ev[2], st);
 
     // ---- K1 ----
@@ -798,6 +816,27 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
         if (split) CK(cudaStreamWaitEvent(st, eng->join, 0), "join");
     }
     CK(cudaGetLastError(), "BAQ launch");
+    if (trace) {
+        // every BAQ read once more through the plain FP64 kernel, writing only its pre-floor qualities, then
+        // the per-read comparison with the FP32 pass (after the replays: the first count pass may still run
+        // beside it, it reads none of the trace)
+        const u32 bwm = std::max(bw_max[0], std::max(bw_max[1], bw_max[2]));
+        const u32 nmax = std::max(n_cls[0], std::max(n_cls[1], n_cls[2]));
+        if (nmax) {
+            const u32 threads = std::min<u32>(baq64_threads(), ((nmax + 127) / 128) * 128);
+            u64 need = baq64_scratch_doubles(threads, max_q, bwm);
+            const u64 budget = (u64(6) << 30) / 8;
+            if (need > budget) need = std::max<u64>(budget, baq64_scratch_doubles(128, max_q, bwm));
+            CK(eng->s64.ensure(need * 8), "FP64 BAQ scratch");
+            eng->s64_doubles = eng->s64.cap / 8;
+            for (int c = 0; c < 3; c++)
+                launch_baq64(b, eng->ref, w, w.baq_list + size_t(c) * R, w.counters + c, n_cls[c], eng->s64.as<double>(),
+                             eng->s64_doubles, max_q, bwm, st, 0, true);
+            for (int c = 0; c < 3; c++)
+                launch_precision(b, w, w.baq_list + size_t(c) * R, w.counters + c, n_cls[c],
+                                 eng->prec_acc.as<PrecisionAcc>(), st);
+        }
+    }
     cudaEventRecord(eng->ev[4], st);
 
     // ---- K3 count (second pass: the replayed reads) + scan ----
@@ -1202,6 +1241,7 @@ fp_status fp_engine_reset(fp_engine *eng) {
     CK(cudaMemsetAsync(eng->tab_cyc.p, 0, size_t(eng->n_rg) * 2 * CYC_DIFF_LEN * sizeof(int), eng->st), "reset");
     eng->staged_bases = 0;
     for (auto &x : eng->co_n) x = 0;  // staged reads of the previous job are dropped
+    if (eng->prec_acc.p) CK(cudaMemsetAsync(eng->prec_acc.p, 0, sizeof(PrecisionAcc), eng->st), "reset");
     CK(cudaStreamSynchronize(eng->st), "reset");
     for (auto &t : eng->out) t = HostTable();
     eng->finalized = false;
@@ -1214,6 +1254,31 @@ fp_status fp_engine_get_stats(const fp_engine *eng, fp_stats *out) {
     if (!eng || !out) return FP_BAD_INPUT;
     *out = eng->stats;
     out->gpu_kernel_launches = g_kernel_launches - eng->launch_base;
+    return FP_OK;
+}
+
+fp_status fp_engine_get_precision_stats(fp_engine *eng, fp_precision_stats *out) {
+    if (!eng || !out) return FP_BAD_INPUT;
+    *out = fp_precision_stats{};
+    if (!eng->prec_acc.p) return FP_OK;
+    CK(cudaSetDevice(eng->device), "set device");
+    PrecisionAcc a{};
+    CK(cudaMemcpyAsync(&a, eng->prec_acc.p, sizeof(a), cudaMemcpyDeviceToHost, eng->st), "D2H");
+    CK(cudaStreamSynchronize(eng->st), "precision stats");
+    static_assert(PREC_BINS == sizeof(out->err_hist) / sizeof(out->err_hist[0]), "histogram bins");
+    out->reads = a.reads;
+    out->reads_without_fp32 = a.reads_without_fp32;
+    out->bases = a.bases;
+    out->bound_violations = a.violations;
+    float f;
+    memcpy(&f, &a.max_err_bits, 4);
+    out->max_abs_error = f;
+    memcpy(&f, &a.max_width_bits, 4);
+    out->max_half_width = f;
+    for (int i = 0; i < PREC_BINS; i++) {
+        out->err_hist[i] = a.err_hist[i];
+        out->width_hist[i] = a.width_hist[i];
+    }
     return FP_OK;
 }
 

@@ -35,7 +35,8 @@ __device__ __forceinline__ double calc_eps(u8 ref, u8 read, u8 q) {
 }
 
 __global__ void __launch_bounds__(THREADS) k_baq64(DevBatch b, DevRef ref, BatchWork w, const u32 *list,
-                                                   const u32 *count, double *scratch, u64 per_thread, int min_bw) {
+                                                   const u32 *count, double *scratch, u64 per_thread, int min_bw,
+                                                   bool trace_only) {
     const u32 tid = blockIdx.x * blockDim.x + threadIdx.x;
     const u32 nthreads = gridDim.x * blockDim.x;
     const u32 n = *count;
@@ -212,9 +213,14 @@ __global__ void __launch_bounds__(THREADS) k_baq64(DevBatch b, DevRef ref, Batch
             }
             max /= sum;
             const u32 qi = qual0 + u32(i - 1);
+            const double tt = double(-4.343) * log(double(1.0) - double(max)) + double(.499);
+            if (trace_only) {  // precision trace: the pre-floor quality only, the batch's results untouched
+                w.trace64[qi] = tt;
+                continue;
+            }
             w.baq_state[qi] = u32(max_k);
             // (int) conversion saturates (+inf -> INT_MAX, NaN -> 0) like the reference's CUDA build
-            const int kq = int(double(-4.343) * log(double(1.0) - double(max)) + double(.499));
+            const int kq = int(tt);
             w.baq_q[qi] = u8(kq > 100 ? 99 : (kq < MIN_BASE_QUAL ? MIN_BASE_QUAL : kq));
             w.baq_amb[qi] = 0;
         }
@@ -238,7 +244,7 @@ void baq64_set_constants(const HmmConst &c) {
 
 void launch_baq64(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
                   u32 max_reads, double *scratch, u64 scratch_doubles, u32 max_qlen, u32 max_bw, cudaStream_t s,
-                  u32 min_bw) {
+                  u32 min_bw, bool trace_only) {
     if (!max_reads) return;
     const u64 row = u64(max_bw * 2 + 1) * 3 + 6;
     const u64 per = u64(max_qlen + 1) * row * 2 + (max_qlen + 2);
@@ -249,7 +255,7 @@ void launch_baq64(const DevBatch &b, const DevRef &ref, const BatchWork &w, cons
     const u64 need = (max_reads + THREADS - 1) / THREADS;
     if (need < blocks) blocks = need;
     if (blocks == 0) return;  // caller guarantees room for at least one block
-    k_baq64<<<u32(blocks), THREADS, 0, s>>>(b, ref, w, list, count, scratch, per, int(min_bw));
+    k_baq64<<<u32(blocks), THREADS, 0, s>>>(b, ref, w, list, count, scratch, per, int(min_bw), trace_only);
     g_kernel_launches++;
 }
 

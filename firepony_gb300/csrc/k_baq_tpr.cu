@@ -564,6 +564,7 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                 u8 amb = 0;
                 int qv = MIN_BASE_QUAL;
                 u32 state = U32_NONE;
+                float tq_trace = 0.0f, lo_trace = 0.0f, hi_trace = 0.0f;  // (precision trace only)
                 if (!(sum > T(0)) || !(sum <= T(3.0e38f)) || max_k < 0) {
                     amb = 7;
                 } else {
@@ -623,6 +624,9 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                         return k > 100 ? 99 : (k < MIN_BASE_QUAL ? MIN_BASE_QUAL : k);
                     };
                     qv = capped(tq);
+                    tq_trace = tq;
+                    lo_trace = lo;
+                    hi_trace = hi;
                     const int flo = capped(lo), fhi = capped(hi);
                     if (qo <= 99) {
                         if ((flo < qo ? flo : qo) != (fhi < qo ? fhi : qo)) amb |= 1;
@@ -633,10 +637,18 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                 w.baq_q[qi] = u8(qv);
                 w.baq_state[qi] = state;
                 w.baq_amb[qi] = amb;
+                if (w.trace32) {
+                    const float nan = __int_as_float(0x7fc00000);
+                    w.trace32[3 * size_t(qi)] = amb == 7 ? nan : tq_trace;
+                    w.trace32[3 * size_t(qi) + 1] = lo_trace;
+                    w.trace32[3 * size_t(qi) + 2] = hi_trace;
+                }
             }
         }
         if (!EXACT && (under || qmax > 93)) {
             for (int i = 0; i < qL; i++) w.baq_amb[qual0 + i] = 7;
+            if (w.trace32)
+                for (int i = 0; i < qL; i++) w.trace32[3 * size_t(qual0 + i)] = __int_as_float(0x7fc00000);
         }
     }
 }

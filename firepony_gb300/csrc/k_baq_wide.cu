@@ -484,6 +484,7 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
                 u8 amb = 0;
                 int qv = MIN_BASE_QUAL;
                 u32 state = U32_NONE;
+                float tq_trace = __int_as_float(0x7fc00000), lo_trace = 0.0f, hi_trace = 0.0f;  // (trace only)
                 if (!valid) {
                     amb = 7;
                 } else {
@@ -511,6 +512,9 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
                         }
                     }
                     qv = capped_q(tq);
+                    tq_trace = tq;
+                    lo_trace = lo;
+                    hi_trace = hi;
                     const int flo = capped_q(lo), fhi = capped_q(hi);
                     if (qo <= 99) {
                         if ((flo < qo ? flo : qo) != (fhi < qo ? fhi : qo)) amb |= 1;
@@ -521,10 +525,18 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
                 w.baq_q[qi] = u8(qv);
                 w.baq_state[qi] = state;
                 w.baq_amb[qi] = amb;
+                if (w.trace32) {
+                    w.trace32[3 * size_t(qi)] = tq_trace;
+                    w.trace32[3 * size_t(qi) + 1] = lo_trace;
+                    w.trace32[3 * size_t(qi) + 2] = hi_trace;
+                }
             }
         }
-        if (has && qmax > 93)
+        if (has && qmax > 93) {
             for (int row = l; row < qL; row += G) w.baq_amb[qual0 + u32(row)] = 7;
+            if (w.trace32)
+                for (int row = l; row < qL; row += G) w.trace32[3 * size_t(qual0 + u32(row))] = __int_as_float(0x7fc00000);
+        }
         __syncwarp();
     }
 }

@@ -35,6 +35,11 @@ struct BatchWork {
                              // [22]/[23] escalations with an undecided MAP state / with undecided qualities only,
                              // [24] work counter of the class-1 replay
     u32 *esc_list;
+    // precision trace (FP_FLAG_PRECISION_TRACE; null otherwise): per base the FP32 kernels' pre-floor MAP
+    // quality t and its certified interval [lo, hi] (t = NaN where the FP32 pass has no value), and the
+    // plain FP64 path's t
+    float *trace32;          // 3 x float per base
+    double *trace64;         // 1 x double per base
     // covariate entries
     u32 *entry_count;        // per read + 1
     u32 *entry_offset;       // per read + 1 (exclusive scan)
@@ -84,7 +89,8 @@ void launch_cap(const DevBatch &b, const BatchWork &w, const u32 *list, const u3
 void baq64_set_constants(const HmmConst &c);
 void launch_baq64(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
                   u32 max_reads, double *scratch, u64 scratch_doubles, u32 max_qlen, u32 max_bw, cudaStream_t s,
-                  u32 min_bw = 0);  // reads of the list with a band narrower than min_bw are skipped
+                  u32 min_bw = 0,  // reads of the list with a band narrower than min_bw are skipped
+                  bool trace_only = false);  // write only w.trace64 (precision trace)
 u64 baq64_scratch_doubles(u32 threads, u32 max_qlen, u32 max_bw);
 u32 baq64_threads();
 
@@ -104,6 +110,16 @@ void launch_baq_exact(const DevBatch &b, const DevRef &ref, const BatchWork &w, 
 void launch_baq_tpr(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
                     u32 max_reads, int band_class, bool exact, u32 *ctr, void *scratch, u64 scratch_bytes, u32 max_q,
                     u32 reads_per_warp, cudaStream_t s);
+
+// k_precision.cu: FP32 vs FP64 MAP quality per BAQ read (precision trace), accumulated over batches
+constexpr int PREC_BINS = 42;  // [0] exactly 0, [1 + k] for 10^(-10 + k/4) <= v < 10^(-10 + (k + 1)/4), [41] v >= 1
+struct PrecisionAcc {
+    unsigned long long reads, reads_without_fp32, bases, violations;
+    unsigned long long err_hist[PREC_BINS], width_hist[PREC_BINS];
+    unsigned int max_err_bits, max_width_bits;  // non-negative floats, ordered as integers
+};
+void launch_precision(const DevBatch &b, const BatchWork &w, const u32 *list, const u32 *count, u32 max_reads,
+                      PrecisionAcc *acc, cudaStream_t s);
 
 // k_covariates.cu
 void launch_cov_count(const DevBatch &b, const BatchWork &w, const Tables &t, cudaStream_t s);

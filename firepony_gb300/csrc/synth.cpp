@@ -116,6 +116,10 @@ uint8_t random_base(Rng &r, double gc) {
 struct QualTable {
     // cumulative distribution of the clamped, rounded normal
     std::vector<double> cdf;
+    // guide[j]: the first index whose cdf value is >= j / GUIDE, where the search for any u in
+    // [j / GUIDE, (j + 1) / GUIDE) starts (the result equals a binary search's, without its branch misses)
+    static constexpr int GUIDE = 4096;
+    std::vector<uint16_t> guide;
     int qmin;
     void build(double mean, double sd, int lo, int hi) {
         qmin = lo;
@@ -130,10 +134,14 @@ struct QualTable {
             cdf[q - lo] = acc;
         }
         for (auto &c : cdf) c /= acc;
+        guide.assign(GUIDE + 1, 0);
+        for (int j = 0; j <= GUIDE; j++)
+            guide[j] = uint16_t(std::lower_bound(cdf.begin(), cdf.end(), double(j) / GUIDE) - cdf.begin());
     }
     uint8_t draw(Rng &r) const {
-        double u = r.uniform();
-        size_t i = std::lower_bound(cdf.begin(), cdf.end(), u) - cdf.begin();
+        const double u = r.uniform();
+        size_t i = guide[size_t(u * GUIDE)];
+        while (i < cdf.size() && cdf[i] < u) i++;
         if (i >= cdf.size()) i = cdf.size() - 1;
         return uint8_t(qmin + int(i));
     }
@@ -257,12 +265,16 @@ int synth_generate_batch(const synth_config *cfg, const synth_reference *ref, ui
     std::vector<uint8_t> syms;  // unpacked read symbols (padded)
     chromosome.reserve(num_reads);
 
+    // per-read scratch, reused across reads
+    struct Ev { uint32_t at; uint32_t op; uint32_t len; };
+    std::vector<Op> ops, merged;
+    std::vector<Ev> evs;
     uint32_t mate_pending = 0;  // paired mode: second read of a pair
     uint32_t pair_contig = 0, pair_r1_start = 0, pair_frag = 0, pair_len = 0;
     for (uint32_t r = 0; r < num_reads; r++) {
         const uint32_t L = cfg->read_lengths[rng.below(cfg->num_read_lengths ? cfg->num_read_lengths : 1)];
         // ---- alignment layout ----
-        std::vector<Op> ops;
+        ops.clear();
         // indels
         int n_indels = 0;
         if (cfg->indel_mode == 0) {
@@ -277,8 +289,7 @@ int synth_generate_batch(const synth_config *cfg, const synth_reference *ref, ui
             if (rng.uniform() < 0.5) clip_left = s; else clip_right = s;
         }
         // read positions (inside the aligned part) that start an indel event
-        struct Ev { uint32_t at; uint32_t op; uint32_t len; };
-        std::vector<Ev> evs;
+        evs.clear();
         const uint32_t core = L - clip_left - clip_right;
         for (int k = 0; k < n_indels; k++) {
             uint32_t at = 10 + uint32_t(rng.below(core > 20 ? core - 20 : 1));
@@ -303,7 +314,7 @@ int synth_generate_batch(const synth_config *cfg, const synth_reference *ref, ui
         if (core > consumed) ops.push_back({0, core - consumed});
         if (clip_right) ops.push_back({4, clip_right});
         // merge adjacent same ops
-        std::vector<Op> merged;
+        merged.clear();
         for (auto &o : ops) {
             if (o.len == 0) continue;
             if (!merged.empty() && merged.back().op == o.op) merged.back().len += o.len; else merged.push_back(o);

@@ -10,8 +10,8 @@ from pathlib import Path
 
 import numpy as np
 
-from .abi import (FP_OK, STATUS_NAMES, FpBatchView, FpOptions, FpRefstoreInfo, FpStats, FpTableView, FP_BAQ_FP32,
-                  FP_BAQ_FP64, table_to_numpy)
+from .abi import (FP_OK, STATUS_NAMES, FpBatchView, FpOptions, FpPrecisionStats, FpRefstoreInfo, FpStats,
+                  FpTableView, FP_BAQ_FP32, FP_BAQ_FP64, table_to_numpy)
 
 _BUILD = Path(__file__).resolve().parent / "_build"
 _lib = None
@@ -21,7 +21,7 @@ EXPORTED = [
     "fp_engine_submit_batch", "fp_engine_finalize", "fp_engine_get_table", "fp_engine_write_report",
     "fp_engine_reset", "fp_engine_get_stats", "fp_engine_debug_last_batch", "fp_report_write", "fp_host_alloc",
     "fp_host_free", "fp_engine_submit_batch_device", "fp_engine_cuda_stream", "fp_sort_entries",
-    "fp_sort_entries_static", "fp_engine_prefetch_batch",
+    "fp_sort_entries_static", "fp_engine_prefetch_batch", "fp_engine_get_precision_stats", "fp_measure_fp32_peak",
 ]
 
 
@@ -55,6 +55,7 @@ def lib():
                                              C.c_int, C.c_int, C.c_int]
         L.fp_engine_reset.argtypes = [C.c_void_p]
         L.fp_engine_get_stats.argtypes = [C.c_void_p, C.POINTER(FpStats)]
+        L.fp_engine_get_precision_stats.argtypes = [C.c_void_p, C.POINTER(FpPrecisionStats)]
         L.fp_engine_debug_last_batch.argtypes = [C.c_void_p] + [C.c_void_p] * 6
         L.fp_report_write.argtypes = [C.c_char_p, C.POINTER(FpTableView), C.POINTER(C.c_char_p), C.c_uint32, C.c_int,
                                       C.c_int, C.c_int, C.c_int]
@@ -65,6 +66,7 @@ def lib():
         L.fp_sort_entries.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_int, C.c_void_p]
         L.fp_sort_entries_static.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_int, C.c_void_p]
         L.fp_host_alloc.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
+        L.fp_measure_fp32_peak.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
         L.fp_host_free.argtypes = [C.c_void_p]
         # reference store (include/firepony_gb300_store.h)
         L.fp_refstore_create.argtypes = [C.c_uint32, C.POINTER(C.c_void_p)]
@@ -122,6 +124,15 @@ def sort_entries(d_in: int, d_out: int, n: int, key_bits: int, stream: int = 0) 
     if rc != FP_OK:
         raise EngineError(f"fp_sort_entries: {STATUS_NAMES.get(rc, rc)}")
 
+
+
+def measure_fp32_peak(device: int = 0, packed: bool = False) -> float:
+    """fp_measure_fp32_peak: the device's FP32 multiply-add throughput in TFLOP/s."""
+    v = C.c_double()
+    rc = lib().fp_measure_fp32_peak(device, int(packed), C.byref(v))
+    if rc != FP_OK:
+        raise EngineError(f"fp_measure_fp32_peak: {STATUS_NAMES.get(rc, rc)}")
+    return v.value
 
 
 class Engine:
@@ -310,6 +321,16 @@ class Engine:
             d[f] = list(v) if hasattr(v, "__len__") else v
         return d
 
+    def precision_stats(self) -> dict:
+        """FP32 vs FP64 pre-floor MAP quality per BAQ read (engine created with FP_FLAG_PRECISION_TRACE)."""
+        s = FpPrecisionStats()
+        self._check(lib().fp_engine_get_precision_stats(self.h, C.byref(s)), "get_precision_stats")
+        d = {}
+        for f, _ in FpPrecisionStats._fields_:
+            v = getattr(s, f)
+            d[f] = list(v) if hasattr(v, "__len__") else v
+        return d
+
     def debug_last_batch(self, batch) -> dict:
         R, Q = batch.num_reads, batch.num_qualities
         d = {"read_status": np.zeros(R, np.uint8), "windows": np.zeros((R, 8), np.uint16),
@@ -345,6 +366,56 @@ class PinnedBatch:
         for p in self._ptrs:
             lib().fp_host_free(p)
         self._ptrs = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PinnedPool:
+    """Page-locked host memory for many batches, taken from a few large fp_host_alloc chunks (one allocation
+    per batch array would cost thousands of page-locking calls for a workload of thousands of batches)."""
+
+    def __init__(self, chunk_bytes: int = 1 << 30):
+        self.chunk_bytes = chunk_bytes
+        self._chunks = []  # (pointer, size)
+        self._cur = None
+        self._off = 0
+        self._size = 0
+
+    def _take(self, nbytes: int) -> int:
+        nbytes = max(1, nbytes)
+        off = (self._off + 255) // 256 * 256
+        if self._cur is None or off + nbytes > self._size:
+            size = max(self.chunk_bytes, nbytes)
+            p = C.c_void_p()
+            if lib().fp_host_alloc(size, C.byref(p)) != FP_OK:
+                raise EngineError("fp_host_alloc failed")
+            self._chunks.append(p)
+            self._cur, self._size, off = p.value, size, 0
+        self._off = off + nbytes
+        return self._cur + off
+
+    def add(self, batch):
+        """Copies a batch into the pool; returns a Batch whose arrays are the pinned copies."""
+        from .synth import BATCH_FIELDS, Batch
+        arrays = {}
+        for name, dt, _ in BATCH_FIELDS:
+            a = batch.arrays[name]
+            addr = self._take(a.nbytes)
+            buf = (C.c_uint8 * max(1, a.nbytes)).from_address(addr)
+            dst = np.frombuffer(buf, dtype=dt, count=len(a))
+            dst[:] = a
+            arrays[name] = dst
+        return Batch(arrays, batch.num_reads, batch.num_cigar_ops, batch.num_read_symbols, batch.num_qualities)
+
+    def close(self):
+        for p in self._chunks:
+            lib().fp_host_free(p)
+        self._chunks = []
+        self._cur = None
 
     def __del__(self):
         try:

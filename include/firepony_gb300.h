@@ -75,6 +75,10 @@ typedef struct {
 /* Test hook: in FP32 mode, run every BAQ read of band width <= 15 through the exact FP64 replay as well
  * (the replay's results replace the FP32 ones), so the replay kernels see the whole workload. */
 #define FP_FLAG_REPLAY_ALL 1u
+/* Measurement: in FP32 mode, also run every BAQ read through the plain FP64 HMM (results unchanged) and
+ * compare the two pre-floor MAP qualities per base; see fp_engine_get_precision_stats. Costs one plain
+ * FP64 BAQ pass per batch. No reference counterpart (the reference has only the FP64 HMM). */
+#define FP_FLAG_PRECISION_TRACE 2u
 
 /* One alignment batch, mirroring alignment_batch_storage<host> (alignment_data.h:125-173). The engine
  * borrows these host buffers only for the duration of fp_engine_submit_batch. */
@@ -142,6 +146,23 @@ typedef struct {
                                             FP32 kernel + capping, the class-1 replay */
 } fp_stats;
 
+/* FP32 vs FP64 per BAQ read (FP_FLAG_PRECISION_TRACE), accumulated since creation or reset. t is the MAP
+ * quality before flooring, -4.343 ln(1 - p_max) + 0.499 (device/baq.cu:673); bases whose FP64 t is 101 or more
+ * (capped to 99 either way) are left out. Histograms are over reads of the per-read maximum: bin 0 holds
+ * exactly 0, bin 1 + k holds 10^(-10 + k/4) <= v < 10^(-10 + (k+1)/4) (k = 0..39, values below 1e-10 in
+ * bin 1), bin 41 holds v >= 1. */
+typedef struct {
+    uint64_t reads;               /* BAQ reads compared */
+    uint64_t reads_without_fp32;  /* reads the FP32 pass handed to the FP64 replay without values (underflow
+                                     guard, qualities above 93) */
+    uint64_t bases;               /* bases compared */
+    uint64_t bound_violations;    /* bases whose FP64 t lies outside the FP32 certified interval (expected 0) */
+    double max_abs_error;         /* largest |t32 - t64| */
+    double max_half_width;        /* widest finite certified half-interval */
+    uint64_t err_hist[42];        /* per read: max |t32 - t64| */
+    uint64_t width_hist[42];      /* per read: max certified half-interval */
+} fp_precision_stats;
+
 typedef enum {
     FP_STAGE_PREP = 0, FP_STAGE_BAQ = 1, FP_STAGE_COVARIATES = 2, FP_STAGE_SORT_REDUCE = 3,
     FP_STAGE_POSTPROCESS = 4, FP_STAGE_H2D = 5, FP_STAGE_D2H = 6, FP_STAGE_OTHER = 7,
@@ -206,6 +227,10 @@ fp_status fp_engine_reset(fp_engine *engine);
 
 fp_status fp_engine_get_stats(const fp_engine *engine, fp_stats *out);
 
+/* The precision trace's accumulated comparison (all zero unless FP_FLAG_PRECISION_TRACE is set). Waits for
+ * the engine's stream. */
+fp_status fp_engine_get_precision_stats(fp_engine *engine, fp_precision_stats *out);
+
 /* Test/debug: copies the per-read and per-base intermediates of the most recent batch to the host.
  * Each pointer may be NULL. Per-read arrays have num_reads entries, per-base arrays num_qualities.
  *   read_status:  0 filtered, 1 active, 2 removed (BAQ window off the contig end)
@@ -244,6 +269,11 @@ fp_status fp_sort_entries_static(const uint64_t *d_in, uint64_t *d_out, uint64_t
 fp_status fp_report_write(const char *path, const fp_table_view *tables, const char *const *rg_names,
                           uint32_t num_rg_names, int disable_rounding, int version_major, int version_minor,
                           int version_rev);
+
+/* Measures the device's FP32 SIMT multiply-add throughput in TFLOP/s (2 flops per multiply-add): one resident
+ * grid of independent fmaf chains (packed = 0) or of packed two-lane __ffma2_rn chains (packed = 1), best of
+ * three timed launches. The roofline denominator of the FP32 BAQ HMM. No reference counterpart. */
+fp_status fp_measure_fp32_peak(int device, int packed, double *tflops);
 
 /* Page-locked host memory for batch buffers (so the H2D copies run at full link speed). Replaces nothing in
  * the reference: its io_thread buffers are pageable (io_thread.cu:44-54). */

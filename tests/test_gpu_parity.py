@@ -69,6 +69,15 @@ def assert_tables_equal(a, b):
         np.testing.assert_allclose(ta["estimated_quality"], tb["estimated_quality"], rtol=REL_TOL, atol=0)
 
 
+def ranges_mask(n, starts, ends):
+    """Boolean mask of length n set on the disjoint half-open ranges [starts[i], ends[i])."""
+    d = np.zeros(n + 1, np.int64)
+    keep = ends > starts
+    np.add.at(d, starts[keep], 1)
+    np.add.at(d, ends[keep], -1)
+    return np.cumsum(d[:n]) > 0
+
+
 def assert_stages_equal(batch, ge, go):
     st_e, st_o = ge["read_status"], go["read_status"]
     np.testing.assert_array_equal(st_e, st_o, err_msg="read status")
@@ -76,17 +85,14 @@ def assert_stages_equal(batch, ge, go):
     np.testing.assert_array_equal(ge["windows"][act][:, :6], go["windows"][act][:, :6], err_msg="windows")
     np.testing.assert_array_equal(ge["windows"][act][:, 6:], go["windows"][act][:, 6:], err_msg="hq windows")
     np.testing.assert_array_equal(ge["hmm"][act], go["hmm"][act], err_msg="hmm window / band / errors")
-    qs, ql = batch["qual_start"], batch["qual_len"]
-    mask = np.zeros(batch.num_qualities, bool)
-    for r in np.nonzero(act)[0]:
-        mask[qs[r]:qs[r] + ql[r]] = True
+    qs, ql = batch["qual_start"].astype(np.int64), batch["qual_len"].astype(np.int64)
+    mask = ranges_mask(batch.num_qualities, qs[act], qs[act] + ql[act])
     np.testing.assert_array_equal(ge["base_flags"][mask], go["base_flags"][mask], err_msg="base flags")
     np.testing.assert_array_equal(ge["baq_tag"][mask], go["baq_tag"][mask], err_msg="BQ tags")
     # fractional errors inside the clipped windows (the engine stores them as the table's float values)
-    win = np.zeros(batch.num_qualities, bool)
-    for r in np.nonzero(act)[0]:
-        x, y = go["windows"][r][0], go["windows"][r][1]
-        win[qs[r] + x:qs[r] + y + 1] = True
+    x = go["windows"][act][:, 0].astype(np.int64)
+    y = go["windows"][act][:, 1].astype(np.int64)
+    win = ranges_mask(batch.num_qualities, qs[act] + x, qs[act] + y + 1)
     fo = go["frac_errors"][win].astype(np.float32).astype(np.float64)
     np.testing.assert_array_equal(ge["frac_errors"][win], fo, err_msg="fractional errors")
 
