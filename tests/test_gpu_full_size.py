@@ -105,7 +105,8 @@ def test_precision_trace_certificate_holds(native):
     assert ps["bound_violations"] == 0
     assert ps["reads"] + ps["reads_without_fp32"] == st["baq_reads"]
     assert ps["reads"] > 0.95 * st["baq_reads"]
-    assert ps["bases"] > 100 * ps["reads"]
+    # about half of a read's bases have an FP64 t below 101 (the rest saturate at 99 either way)
+    assert ps["bases"] > 20 * ps["reads"]
     assert sum(ps["err_hist"]) == ps["reads"] == sum(ps["width_hist"])
     # FP32 against FP64: far inside a quality unit
     assert 0 < ps["max_abs_error"] < 0.05
