@@ -30,6 +30,7 @@ ENGINE_UNITS = [
     ("k_prep.cu", []),
     ("k_baq64.cu", ["-fmad=false"]),   # FP64 HMM: bit-exact replay of the reference's operation order
     ("k_baq_tpr.cu", []),
+    ("k_baq_seg.cu", []),               # band class 0 FP32 (checkpointed forward rows, packed pairs)
     ("k_baq_exact.cu", ["-fmad=false"]),  # exact FP64 replay (explicit rounding intrinsics throughout)
     ("k_baq_wide.cu", []),              # FP32 certified HMM for bands wider than 15
     ("k_covariates.cu", []),

@@ -278,6 +278,7 @@ static fp_status create_impl(const fp_options *o, fp_engine **out) {
     eng->hmm.gap_open = pow(10.0, (-40.0) / 10.);
     baq64_set_constants(eng->hmm);
     baq_tpr_set_constants(eng->hmm);
+    baq_seg_set_constants(eng->hmm);
     baq_exact_set_constants(eng->hmm);
     baq_wide_set_constants(eng->hmm);
     EmpConst ec;
@@ -739,7 +740,11 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
         auto run_fp32 = [&](int c, cudaStream_t cs, void *scr, u64 scr_bytes, u32 *ctr) {
             const u32 *list = sorted_lists + size_t(c) * R;
             if (c == 0) cudaEventRecord(eng->ev[10], cs);
-            launch_baq_tpr(b, eng->ref, w, list, w.counters + c, n_cls[c], c, false, ctr, scr, scr_bytes, max_q, 32, cs);
+            if (c == 0)
+                launch_baq_seg(b, eng->ref, w, list, w.counters + c, n_cls[c], ctr, scr, scr_bytes, max_q, cs);
+            else
+                launch_baq_tpr(b, eng->ref, w, list, w.counters + c, n_cls[c], c, false, ctr, scr, scr_bytes, max_q, 32,
+                               cs);
             if (c == 0) { cudaEventRecord(eng->ev[11], cs); timed_main = true; }
             launch_cap(b, w, list, w.counters + c, 0, cs, n_cls[c]);
         };

@@ -600,9 +600,25 @@ __global__ void __launch_bounds__(PREP_WARPS * 32) k_prep(DevBatch b, DevRef ref
             // read_flat_baq (device/baq.cu:842-868)
             for (u32 i = wcl.x + u32(lane); i <= wcl.y; i += 32) w.tag[qs + i] = NO_BAQ_UNCERTAINTY;
         }
+        // a reference N inside the HMM window (emission 1 for every query base) takes a read of band class 0 to
+        // the general kernel of class 1: the class-0 kernel selects emissions by symbol equality alone
+        bool ref_n = false;
+        if (status == RS_ACTIVE && nerr != 0 && bw <= 7 && g) {
+            int refLen = int(hw.y) - int(hw.x) + 1;
+            u64 off;
+            if (hw.x < 0 && rd.astart < baq_abs(hw.x)) {
+                off = 0;
+                refLen--;
+            } else {
+                off = u64(u32(rd.astart + u32(int(hw.x))));
+            }
+            bool any = false;
+            for (int k = lane; k < refLen; k += 32) any |= contig_at(*g, off + u64(k)) == IUPAC_N;
+            ref_n = __any_sync(WFULL, any);
+        }
         if (lane == 0 && status == RS_ACTIVE && nerr != 0) {
             // BAQ work list by band class: 0 -> bw <= 7, 1 -> bw <= 15, 2 -> wider
-            const u32 cls = bw <= 7 ? 0 : (bw <= 15 ? 1 : 2);
+            const u32 cls = bw <= 7 ? (ref_n ? 1 : 0) : (bw <= 15 ? 1 : 2);
             const u32 slot = atomicAdd(&w.counters[cls], 1u);
             w.baq_list[size_t(cls) * b.R + slot] = r;
             // band cells of the read's HMM (rows 1..qL, reference positions max(1, i-bw)..min(refLen, i+bw)),

@@ -94,6 +94,11 @@ void launch_baq64(const DevBatch &b, const DevRef &ref, const BatchWork &w, cons
 u64 baq64_scratch_doubles(u32 threads, u32 max_qlen, u32 max_bw);
 u32 baq64_threads();
 
+// k_baq_seg.cu (band class 0, FP32 certified: thread per read, packed FP32 pairs, checkpointed forward rows)
+void baq_seg_set_constants(const HmmConst &c);
+u64 baq_seg_scratch_bytes(u32 max_q);
+void launch_baq_seg(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
+                    u32 max_reads, u32 *ctr, void *scratch, u64 scratch_bytes, u32 max_q, cudaStream_t s);
 // k_baq_tpr.cu (thread per read, band in registers; FP32 certified or exact FP64)
 void baq_tpr_set_constants(const HmmConst &c);
 // k_baq_exact.cu (exact FP64 replay, a group of lanes per read)

@@ -335,3 +335,35 @@ def test_prefetched_submits(native):
     assert_tables_equal(t1, to)
     assert_tables_equal(t2, to)
     assert FpBatchView is not None
+
+
+def test_reference_n_in_hmm_windows(native):
+    """Reads whose HMM reference window holds an N (emission 1 whatever the query base) next to reads without
+    one, over runs of N in the reference: the band-class-0 reads with an N go to the general FP32 kernel, the
+    others to the class-0 kernel; tables and per-stage intermediates equal the oracle's, in FP32 and FP64."""
+    from tests.edge_cases import IUPAC, build_batch, make_reference, read_from_cigar
+    from firepony_gb300.synth import pack4
+    rng = np.random.default_rng(5)
+    ref = list(make_reference(6000, seed=11))
+    for a, n in ((1000, 1), (1500, 3), (2000, 12), (3000, 2)):
+        ref[a:a + n] = ["N"] * n
+    ref = "".join(ref)
+    read_src = ref.replace("N", "A")  # the reads carry a base where the reference has N
+    recs = []
+    for pos in list(range(900, 1100, 9)) + list(range(1400, 1560, 7)) + list(range(1900, 2060, 11)) + \
+            list(range(2900, 3050, 13)) + [4000, 4100, 4200]:
+        for cigar, subs in (("60M", (10, 40)), ("30M2D30M", (5,)), ("25M1I34M", (50,))):
+            seq, q, span = read_from_cigar(read_src, pos, cigar, rng, subs, 30)
+            recs.append(dict(pos=pos, cigar=cigar, seq=seq, quals=q, flags=0, mapq=60, rg=0, chrom=0, span=span))
+    batch = build_batch(recs)
+    syms = np.array([IUPAC[c] for c in ref], np.uint8)
+    contigs = [(pack4(syms), len(ref))]
+    sites = [(np.zeros(0, np.uint32), np.zeros(0, np.uint32))]
+    to, so, go = run_oracle(contigs, [batch], 1, sites)
+    for mode in ("fp32", "fp64"):
+        te, se, ge = run_engine(contigs, [batch], 1, mode, sites)
+        assert se["baq_reads"] == so["baq_reads"] > 100
+        if mode == "fp32":
+            assert se["baq_reads_by_band"][1] > 0  # the reads with an N in their window
+        assert_stages_equal(batch, ge, go)
+        assert_tables_equal(te, to)
