@@ -71,6 +71,8 @@ def parse():
     ap.add_argument("--serve-rate", type=float, default=20.0, help="job arrivals per second (Poisson)")
     ap.add_argument("--serve-slots", type=int, default=3, help="engines of the job server")
     ap.add_argument("--serve-max-reads", type=int, default=5_000_000, help="largest job (log-uniform from 1000)")
+    ap.add_argument("--only", default="", choices=["", "batched", "serving", "configs", "refstore", "sort"],
+                    help="run one independent leg alone and print its result (for profiling that leg)")
     ap.add_argument("--serve-hbm-gb", type=float, default=10.0,
                     help="job server admission budget: estimated device memory of the jobs running together "
                          "(0: slots only)")
@@ -444,11 +446,13 @@ def _measured_peak_gbs() -> float:
 
 
 def run_sort(args):
-    """The radix sort primitive (fp_sort_entries: stable LSD passes of 8-bit digits over packed 64-bit entries,
-    dense key in the high 32 bits) on `--sort-entries` random entries with 29-bit keys (the context table's key
-    width), inputs in HBM and larger than L2. Algorithmic bytes = entries x 8 B x 2 (read + write) x passes
-    (the histogram reads are not counted), against the measured HBM copy bandwidth. CUDA events on the stream
-    the sort is launched on; the result is checked for sortedness and for being a permutation."""
+    """The radix sort primitive (fp_sort_entries: stable LSD passes of digits of at most 10 bits over packed
+    64-bit entries, dense key in the high 32 bits; 29-bit keys take 3 passes) on `--sort-entries` random entries
+    with 29-bit keys (the context table's key width), inputs in HBM and larger than L2. Algorithmic bytes follow
+    the 8-bit-digit model whatever digit width the kernels use: entries x 8 B x 2 (read + write) x ceil(29 / 8)
+    passes, against the measured HBM copy bandwidth. The kernels move entries x 8 B x 3 per pass they run (a
+    counting read, then a read and a write). CUDA events on the stream the sort is launched on; the result is
+    checked for sortedness and for being a permutation."""
     import numpy as np
     import torch
     from firepony_gb300.engine import sort_entries
@@ -471,12 +475,14 @@ def run_sort(args):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
     passes = (key_bits + 7) // 8
+    kernel_passes = (key_bits + 9) // 10
     algo = n * 8 * 2 * passes
     k = (dst >> 32)
     ok = bool((k[1:] >= k[:-1]).all().item()) and int(dst.sum().item()) == int(src.sum().item())
     peak = _measured_peak_gbs()
     gbs = algo / (ms * 1e-3) / 1e9
-    return {"entries": n, "key_bits": key_bits, "passes": passes, "ms": ms, "algorithmic_gb": algo / 1e9,
+    return {"entries": n, "key_bits": key_bits, "passes": passes, "kernel_passes": kernel_passes,
+            "kernel_gb": n * 8 * 3 * kernel_passes / 1e9, "ms": ms, "algorithmic_gb": algo / 1e9,
             "achieved_gbs": gbs, "peak_gbs": peak, "frac": gbs / peak if peak else None, "sorted": ok,
             "entries_per_s": n / (ms * 1e-3)}
 
@@ -839,6 +845,13 @@ def main():
         print(json.dumps(line))
         return 0
 
+    if args.only:
+        if rank != 0:
+            return 0
+        legs = {"batched": run_batched, "serving": run_serving, "configs": run_config_legs, "refstore": run_refstore,
+                "sort": run_sort}
+        print(json.dumps({"leg": args.only, "result": legs[args.only](args)}))
+        return 0
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")

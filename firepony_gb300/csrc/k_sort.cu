@@ -99,132 +99,229 @@ void scan_rec(const u32 *in, u32 *out, u64 n, u32 *tmp, cudaStream_t s) {
 }
 
 // ---- radix sort ----
-// A tile of RS_TILE keys per block; warp w of the block takes the tile's w-th run of RS_WARP_KEYS consecutive
-// keys, 32 per round, so tile order is (warp, round, lane). The scatter pass ranks each key among the equal
-// digits before it in tile order (warp-private counters, no block barrier per round), reorders the tile by
-// digit in shared memory, and writes each digit's run with consecutive threads on consecutive addresses.
+// Stable LSD passes over the key bits [32, 32 + key_bits) of packed 64-bit entries, with digits of at most
+// RS_MAX_BITS bits: a key width of b bits takes ceil(b / 10) passes of near-equal digit widths (29 bits: 10, 10,
+// 9). Each pass is three kernels:
+//   k_rs_count   digit counts per chunk of the input (a chunk is a run of consecutive tiles),
+//   k_rs_colscan the chunk counts turned into each chunk's first output position per digit (in place),
+//   k_rs_scatter one CTA per chunk walks its tiles in order; per tile it ranks every key among the equal digits
+//                before it in tile order, reorders the tile by digit in shared memory and writes each digit's
+//                run with consecutive threads on consecutive addresses.
+// A chunk's tiles are processed in order by one CTA that carries each digit's next output position from tile
+// to tile, so the scan runs over one row of digit counts per chunk (about two per SM) instead of one per tile.
 constexpr int RS_THREADS = 256;
 constexpr int RS_WARPS = RS_THREADS / 32;
-constexpr int RS_ROUNDS = 16;
+constexpr int RS_ROUNDS = 16;                      // keys per thread and tile
 constexpr int RS_WARP_KEYS = 32 * RS_ROUNDS;
-constexpr int RS_TILE = RS_THREADS * RS_ROUNDS;
+constexpr int RS_TILE = RS_THREADS * RS_ROUNDS;    // 4096 keys
+constexpr int RS_MAX_BITS = 10;
+constexpr int RS_MAXD = 1 << RS_MAX_BITS;
+constexpr int RS_COUNT_SPLIT = 3;                  // counting CTAs per chunk
+constexpr int RS_CTAS_PER_SM = 2;                  // scatter CTAs resident per SM (shared memory bound)
 
-// The digit of a pass: key bits [shift, shift + 8) of the entry, cut at key_bits so that key bits above the
-// sorted width never decide the order (the last pass of a width that is not a multiple of 8 takes fewer bits).
-__device__ __forceinline__ u32 digit_mask(int shift, int key_bits) {
-    const int w = key_bits - shift;
-    return w >= 8 ? 0xFFu : ((1u << w) - 1u);
-}
+// shared memory of k_rs_scatter (88 KB)
+struct RsScatterSmem {
+    u64 buf[RS_TILE];                  // the tile ordered by digit
+    u32 peers[RS_WARPS][RS_MAXD];      // per warp: lanes of the current round holding the digit (zero between rounds)
+    u16 cnt[RS_WARPS][RS_MAXD];        // per warp: keys of the digit so far in this tile, then the warp's first slot
+    u32 next[RS_MAXD];                 // output position of the chunk's next key of the digit
+    u32 off[RS_MAXD];                  // output position of tile slot p (digit d) = off[d] + p
+};
+
 __device__ __forceinline__ u32 digit_of(u64 v, int shift, u32 mask) { return u32(v >> (32 + shift)) & mask; }
 
-// The lanes of the warp holding a key with digit d (the caller's own lane included), from one ballot per digit
-// bit; lanes without a key form their own group. Votes run on the integer pipe, where a match instruction
-// would queue on the warp-divergence unit (measured: that unit 84-89% busy, the sort issue-bound on it).
-__device__ __forceinline__ u32 digit_peers(u32 d, bool valid) {
-    const u32 vm = __ballot_sync(FULL, valid);
-    u32 peers = valid ? vm : ~vm;
+// Digit counts of one chunk: RS_COUNT_SPLIT CTAs per chunk each count a third of its keys into warp-private
+// shared counters and add them to the chunk's row of `hist` (zeroed by the caller).
+__global__ void __launch_bounds__(RS_THREADS) k_rs_count(const u64 *in, u64 n, int shift, int bits, u32 tpc,
+                                                         u32 *hist) {
+    __shared__ u32 h[RS_WARPS][RS_MAXD];
+    const int D = 1 << bits;
+    const u32 mask = u32(D - 1);
+    const int warp = threadIdx.x >> 5;
+    for (int j = threadIdx.x; j < RS_WARPS * RS_MAXD; j += RS_THREADS) (&h[0][0])[j] = 0;
+    __syncthreads();
+    const u32 c = blockIdx.x / RS_COUNT_SPLIT, part = blockIdx.x % RS_COUNT_SPLIT;
+    const u64 k0 = u64(c) * tpc * RS_TILE;
+    const u64 k1 = k0 + u64(tpc) * RS_TILE < n ? k0 + u64(tpc) * RS_TILE : n;
+    const u64 len = k1 - k0;
+    const u64 a = k0 + len * part / RS_COUNT_SPLIT, b = k0 + len * (part + 1) / RS_COUNT_SPLIT;
+    constexpr int U = 8;
+    u64 i = a + threadIdx.x;
+    for (; i + u64(U - 1) * RS_THREADS < b; i += u64(U) * RS_THREADS) {
+        u64 x[U];
 #pragma unroll
-    for (int b = 0; b < 8; b++) {
-        const bool bit = (d >> b) & 1u;
-        const u32 m = __ballot_sync(FULL, bit);
-        peers &= bit ? m : ~m;
+        for (int j = 0; j < U; j++) x[j] = in[i + u64(j) * RS_THREADS];
+#pragma unroll
+        for (int j = 0; j < U; j++) atomicAdd(&h[warp][digit_of(x[j], shift, mask)], 1u);
     }
-    return peers;
+    for (; i < b; i += RS_THREADS) atomicAdd(&h[warp][digit_of(in[i], shift, mask)], 1u);
+    __syncthreads();
+    for (int d = threadIdx.x; d < D; d += RS_THREADS) {
+        u32 s = 0;
+#pragma unroll
+        for (int w = 0; w < RS_WARPS; w++) s += h[w][d];
+        if (s) atomicAdd(&hist[u64(c) * D + d], s);
+    }
 }
 
-__global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const u64 *in, u64 n, int shift, int key_bits, u32 *hist,
-                                                        u32 nblocks) {
-    const u32 dmask = digit_mask(shift, key_bits);
-    __shared__ u32 h[RS_WARPS][256];  // per warp: only its own lanes update it
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int j = threadIdx.x; j < RS_WARPS * 256; j += RS_THREADS) (&h[0][0])[j] = 0;
+// Column scan of the chunk counts, in place: hist[c][d] becomes the number of keys with digit d in chunks before
+// c; totals[d] = keys with digit d. A CTA takes 32 digits (a lane each) and its 32 warps split the chunk rows.
+__global__ void __launch_bounds__(1024) k_rs_colscan(u32 *hist, u32 G, int D, u32 *totals) {
+    __shared__ u32 part[32][33];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int d = blockIdx.x * 32 + lane;
+    const u32 rpw = (G + 31) / 32;
+    const u32 r0 = u32(w) * rpw < G ? u32(w) * rpw : G;
+    const u32 r1 = r0 + rpw < G ? r0 + rpw : G;
+    u32 s = 0;
+    if (d < D)
+        for (u32 r = r0; r < r1; r++) s += hist[u64(r) * D + d];
+    part[w][lane] = s;
     __syncthreads();
-    const u64 wbase = u64(blockIdx.x) * RS_TILE + u64(warp) * RS_WARP_KEYS;
-    u64 v[RS_ROUNDS];
-#pragma unroll
-    for (int r = 0; r < RS_ROUNDS; r++) {
-        const u64 i = wbase + u64(r) * 32 + lane;
-        v[r] = i < n ? in[i] : 0;
+    u32 p = 0;
+    for (int k = 0; k < w; k++) p += part[k][lane];
+    if (d < D) {
+        for (u32 r = r0; r < r1; r++) {
+            const u32 x = hist[u64(r) * D + d];
+            hist[u64(r) * D + d] = p;
+            p += x;
+        }
+        if (w == 31) totals[d] = p;
     }
-#pragma unroll
-    for (int r = 0; r < RS_ROUNDS; r++) {
-        const bool valid = wbase + u64(r) * 32 + lane < n;
-        const u32 d = digit_of(v[r], shift, dmask);
-        const u32 peers = digit_peers(d, valid);
-        // one update per distinct digit (distinct addresses within the instruction)
-        if (valid && int(__ffs(peers)) - 1 == lane) h[warp][d] += u32(__popc(peers));
-        __syncwarp();  // the next round's updater of a digit may be another lane
-    }
-    __syncthreads();
-    u32 t = 0;
-#pragma unroll
-    for (int w = 0; w < RS_WARPS; w++) t += h[w][threadIdx.x];
-    hist[u64(threadIdx.x) * nblocks + blockIdx.x] = t;
 }
 
-__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const u64 *in, u64 n, int shift, int key_bits,
-                                                           const u32 *offs, u32 nblocks, u64 *out) {
-    const u32 dmask = digit_mask(shift, key_bits);
-    __shared__ u64 buf[RS_TILE];            // the tile ordered by digit
-    __shared__ u32 wcnt[RS_WARPS][256];     // per warp: digit counts, then the warp's first slot per digit
-    __shared__ u32 tstart[256];             // first slot of each digit in the ordered tile
-    __shared__ u32 gbase[256];              // global position of this tile's first key of each digit
+// Loads tile t of the input; in a partial tile the keys past n are left unset (they are never ranked).
+__device__ __forceinline__ void rs_load_tile(const u64 *in, u64 n, u64 t, int warp, int lane, u64 (&v)[RS_ROUNDS]) {
+    const u64 wbase = t * RS_TILE + u64(warp) * RS_WARP_KEYS + lane;
+    if (t * RS_TILE + RS_TILE <= n) {
+#pragma unroll
+        for (int r = 0; r < RS_ROUNDS; r++) v[r] = in[wbase + u64(r) * 32];
+    } else {
+#pragma unroll
+        for (int r = 0; r < RS_ROUNDS; r++) v[r] = wbase + u64(r) * 32 < n ? in[wbase + u64(r) * 32] : 0;
+    }
+}
+
+__global__ void __launch_bounds__(RS_THREADS, RS_CTAS_PER_SM)
+    k_rs_scatter(const u64 *in, u64 n, int shift, int bits, const u32 *colpre, const u32 *totals, u32 tpc,
+                 u64 *out) {
+    extern __shared__ __align__(16) unsigned char rs_smem[];
+    RsScatterSmem &S = *reinterpret_cast<RsScatterSmem *>(rs_smem);
+    const int D = 1 << bits;
+    const u32 mask = u32(D - 1);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const u32 lt = (1u << lane) - 1;
-    for (int j = threadIdx.x; j < RS_WARPS * 256; j += RS_THREADS) (&wcnt[0][0])[j] = 0;
-    gbase[threadIdx.x] = offs[u64(threadIdx.x) * nblocks + blockIdx.x];
-    __syncthreads();
-    const u64 tile0 = u64(blockIdx.x) * RS_TILE;
-    const u64 wbase = tile0 + u64(warp) * RS_WARP_KEYS;
-    u64 v[RS_ROUNDS];
-    u32 rank[RS_ROUNDS / 2];  // per key: the warp's earlier keys with the same digit (< 512), two per word
-#pragma unroll
-    for (int r = 0; r < RS_ROUNDS; r++) {
-        const u64 i = wbase + u64(r) * 32 + lane;
-        v[r] = i < n ? in[i] : 0;
-    }
-#pragma unroll
-    for (int r = 0; r < RS_ROUNDS; r++) {
-        const bool valid = wbase + u64(r) * 32 + lane < n;
-        const u32 d = digit_of(v[r], shift, dmask);
-        const u32 peers = digit_peers(d, valid);
-        const u32 before = valid ? wcnt[warp][d] : 0u;  // the digit's peers read one word together
-        const u32 rk = before + u32(__popc(peers & lt));
-        if (r & 1) rank[r >> 1] |= rk << 16;
-        else rank[r >> 1] = rk;
-        __syncwarp();
-        if (valid && int(__ffs(peers)) - 1 == lane) wcnt[warp][d] = before + u32(__popc(peers));
-        __syncwarp();
-    }
-    __syncthreads();
+    const u32 lt = (1u << lane) - 1, lanebit = 1u << lane;
+    for (int j = threadIdx.x; j < RS_WARPS * RS_MAXD; j += RS_THREADS) (&S.peers[0][0])[j] = 0;
     {
-        // thread d: the digit's count over the warps (warp-major within the digit), then its place in the tile
-        const u32 d = threadIdx.x;
-        u32 run = 0;
+        // the chunk's first output position per digit: keys of smaller digits + keys of the digit in earlier
+        // chunks (thread t takes digits 4t..4t+3)
+        u32 t4[4], sum = 0;
 #pragma unroll
-        for (int w = 0; w < RS_WARPS; w++) {
-            const u32 c = wcnt[w][d];
-            wcnt[w][d] = run;
-            run += c;
+        for (int k = 0; k < 4; k++) {
+            const int d = 4 * threadIdx.x + k;
+            t4[k] = d < D ? totals[d] : 0u;
+            sum += t4[k];
         }
         u32 total;
-        const u32 start = block_exclusive_scan(run, &total);
-        tstart[d] = start;
+        u32 p = block_exclusive_scan(sum, &total);
 #pragma unroll
-        for (int w = 0; w < RS_WARPS; w++) wcnt[w][d] += start;
+        for (int k = 0; k < 4; k++) {
+            const int d = 4 * threadIdx.x + k;
+            if (d < D) S.next[d] = p + colpre[u64(blockIdx.x) * D + d];
+            p += t4[k];
+        }
     }
-    __syncthreads();
+    const u64 ntiles = (n + RS_TILE - 1) / RS_TILE;
+    const u64 t_begin = u64(blockIdx.x) * tpc;
+    const u64 t_end = t_begin + tpc < ntiles ? t_begin + tpc : ntiles;
+    u64 nxt[RS_ROUNDS];
+    rs_load_tile(in, n, t_begin, warp, lane, nxt);
+    u32 *peers = S.peers[warp];
+    u16 *cnt = S.cnt[warp];
+    for (u64 t = t_begin; t < t_end; t++) {
+        u64 v[RS_ROUNDS];
 #pragma unroll
-    for (int r = 0; r < RS_ROUNDS; r++) {
-        const u64 i = wbase + u64(r) * 32 + lane;
-        if (i < n) buf[wcnt[warp][digit_of(v[r], shift, dmask)] + ((rank[r >> 1] >> ((r & 1) * 16)) & 0xFFFFu)] = v[r];
-    }
-    __syncthreads();
-    const u32 tile_n = u32(n - tile0 < u64(RS_TILE) ? n - tile0 : u64(RS_TILE));
-    for (u32 p = threadIdx.x; p < tile_n; p += RS_THREADS) {
-        const u64 key = buf[p];
-        const u32 d = digit_of(key, shift, dmask);
-        out[gbase[d] + (p - tstart[d])] = key;
+        for (int r = 0; r < RS_ROUNDS; r++) v[r] = nxt[r];
+        if (t + 1 < t_end) rs_load_tile(in, n, t + 1, warp, lane, nxt);  // in flight while this tile is ranked
+        const u64 tile0 = t * RS_TILE;
+        const u32 tile_n = u32(n - tile0 < u64(RS_TILE) ? n - tile0 : u64(RS_TILE));
+        const u32 wkeys = tile_n > u32(warp) * RS_WARP_KEYS ? tile_n - u32(warp) * RS_WARP_KEYS : 0u;
+        // clear the counters (the previous tile's output loop no longer reads them)
+        for (int j = threadIdx.x; j < RS_WARPS * RS_MAXD / 2; j += RS_THREADS)
+            reinterpret_cast<u32 *>(&S.cnt[0][0])[j] = 0;
+        __syncthreads();
+        // rank: per round, the lanes with equal digits find each other through one shared-memory OR per lane;
+        // the lowest of them advances the warp's count for the digit and clears the mask
+        u32 rank[RS_ROUNDS / 2];
+#pragma unroll
+        for (int r = 0; r < RS_ROUNDS; r++) {
+            const bool valid = u32(r) * 32 + u32(lane) < wkeys;
+            const u32 d = digit_of(v[r], shift, mask);
+            if (valid) atomicOr(&peers[d], lanebit);
+            __syncwarp();
+            u32 pm = 0, before = 0;
+            if (valid) {
+                pm = peers[d];
+                before = cnt[d];
+            }
+            __syncwarp();
+            if (valid && (pm & lt) == 0) {
+                cnt[d] = u16(before + u32(__popc(pm)));
+                peers[d] = 0;
+            }
+            __syncwarp();
+            const u32 rk = before + u32(__popc(pm & lt));
+            if (r & 1) rank[r >> 1] |= rk << 16;
+            else rank[r >> 1] = rk;
+        }
+        __syncthreads();
+        {
+            // per digit (thread t: digits 4t..4t+3): the warps' counts become their first slots within the
+            // digit, the tile's digit counts are scanned into the digits' first slots in the tile
+            u32 tc[4], sum = 0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int d = 4 * threadIdx.x + k;
+                u32 acc = 0;
+                if (d < D) {
+#pragma unroll
+                    for (int w = 0; w < RS_WARPS; w++) {
+                        const u32 c = S.cnt[w][d];
+                        S.cnt[w][d] = u16(acc);
+                        acc += c;
+                    }
+                }
+                tc[k] = acc;
+                sum += acc;
+            }
+            u32 total;
+            u32 start = block_exclusive_scan(sum, &total);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int d = 4 * threadIdx.x + k;
+                if (d < D) {
+#pragma unroll
+                    for (int w = 0; w < RS_WARPS; w++) S.cnt[w][d] = u16(S.cnt[w][d] + start);
+                    const u32 nd = S.next[d];
+                    S.off[d] = nd - start;
+                    S.next[d] = nd + tc[k];
+                }
+                start += tc[k];
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < RS_ROUNDS; r++) {
+            if (u32(r) * 32 + u32(lane) < wkeys) {
+                const u32 d = digit_of(v[r], shift, mask);
+                S.buf[u32(cnt[d]) + ((rank[r >> 1] >> ((r & 1) * 16)) & 0xFFFFu)] = v[r];
+            }
+        }
+        __syncthreads();
+        for (u32 p = threadIdx.x; p < tile_n; p += RS_THREADS) {
+            const u64 key = S.buf[p];
+            out[u32(S.off[digit_of(key, shift, mask)] + p)] = key;
+        }
     }
 }
 
@@ -265,6 +362,63 @@ __global__ void k_fold(const u64 *s, u64 n, const u32 *heads, const u32 *num_hea
     }
 }
 
+
+// Sort geometry for n entries on the current device: tiles of RS_TILE keys, chunks of `tpc` consecutive tiles,
+// one scatter CTA per chunk (at most RS_CTAS_PER_SM per SM, so every chunk's CTA is resident at once).
+struct RsPlan {
+    u64 ntiles;
+    u32 tpc, chunks;
+};
+
+int device_sm_count() {
+    static int cached[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    if (!cached[dev]) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 152;
+        cached[dev] = v;
+    }
+    return cached[dev];
+}
+
+RsPlan rs_plan(u64 n) {
+    RsPlan p;
+    p.ntiles = (n + RS_TILE - 1) / RS_TILE;
+    const u64 max_chunks = u64(device_sm_count()) * RS_CTAS_PER_SM;
+    const u64 g0 = p.ntiles < max_chunks ? p.ntiles : max_chunks;
+    p.tpc = u32((p.ntiles + g0 - 1) / (g0 ? g0 : 1));
+    p.chunks = p.tpc ? u32((p.ntiles + p.tpc - 1) / p.tpc) : 0u;
+    return p;
+}
+
+// Digit widths of the passes for a key width: ceil(bits / RS_MAX_BITS) passes, widths differing by at most one.
+int rs_passes(int key_bits, int *width) {
+    if (key_bits <= 0) return 0;
+    const int passes = (key_bits + RS_MAX_BITS - 1) / RS_MAX_BITS;
+    for (int p = 0; p < passes; p++) width[p] = key_bits / passes + (p < key_bits % passes ? 1 : 0);
+    return passes;
+}
+
+void rs_pass(const u64 *src, u64 *dst, u64 n, int shift, int bits, const RsPlan &plan, void *tmp, cudaStream_t s) {
+    static bool attr_set[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+        cudaFuncSetAttribute(k_rs_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(RsScatterSmem)));
+        attr_set[dev] = true;
+    }
+    const int D = 1 << bits;
+    u32 *hist = reinterpret_cast<u32 *>(tmp);
+    u32 *totals = hist + u64(plan.chunks) * RS_MAXD;
+    cudaMemsetAsync(hist, 0, u64(plan.chunks) * D * sizeof(u32), s);
+    k_rs_count<<<plan.chunks * RS_COUNT_SPLIT, RS_THREADS, 0, s>>>(src, n, shift, bits, plan.tpc, hist);
+    k_rs_colscan<<<(D + 31) / 32, 1024, 0, s>>>(hist, plan.chunks, D, totals);
+    k_rs_scatter<<<plan.chunks, RS_THREADS, sizeof(RsScatterSmem), s>>>(src, n, shift, bits, hist, totals, plan.tpc,
+                                                                        dst);
+    g_kernel_launches += 3;
+}
+
 }  // namespace
 
 size_t scan_tmp_bytes(u64 n) {
@@ -283,9 +437,9 @@ void launch_exclusive_scan(const u32 *in, u32 *out, u64 n, void *tmp, cudaStream
 }
 
 size_t radix_tmp_bytes(u64 n) {
-    const u64 nblocks = (n + RS_TILE - 1) / RS_TILE + 1;
-    const u64 hist = nblocks * 256;
-    return size_t(2 * (hist + 1)) * sizeof(u32) + scan_tmp_bytes(hist) + 256;
+    // one row of digit counts per chunk, then the digit totals
+    const RsPlan plan = rs_plan(n);
+    return size_t(u64(plan.chunks) * RS_MAXD + RS_MAXD) * sizeof(u32) + 256;
 }
 
 size_t fold_tmp_bytes(u64 n) { return size_t(3 * (n + 1)) * sizeof(u32) + scan_tmp_bytes(n) + 256; }
@@ -294,21 +448,14 @@ void launch_radix_sort(u64 *keys, u64 *alt, u64 n, int key_bits, void *tmp, size
                        cudaStream_t s) {
     (void)tmp_bytes;
     u64 *src = keys, *dst = alt;
-    if (n > 1) {
-        const u32 nblocks = u32((n + RS_TILE - 1) / RS_TILE);
-        const u64 hist_n = u64(nblocks) * 256;
-        u32 *hist = reinterpret_cast<u32 *>(tmp);
-        u32 *offs = hist + hist_n + 1;
-        void *stmp = offs + hist_n + 1;
-        for (int shift = 0; shift < key_bits; shift += 8) {
-            k_rs_hist<<<nblocks, RS_THREADS, 0, s>>>(src, n, shift, key_bits, hist, nblocks);
-            scan_rec(hist, offs, hist_n, reinterpret_cast<u32 *>(stmp), s);
-            k_rs_scatter<<<nblocks, RS_THREADS, 0, s>>>(src, n, shift, key_bits, offs, nblocks, dst);
-            g_kernel_launches += 2;
-            u64 *t = src;
-            src = dst;
-            dst = t;
-        }
+    int width[4];
+    const int passes = n > 1 ? rs_passes(key_bits, width) : 0;
+    const RsPlan plan = rs_plan(n);
+    for (int p = 0, shift = 0; p < passes; shift += width[p], p++) {
+        rs_pass(src, dst, n, shift, width[p], plan, tmp, s);
+        u64 *t = src;
+        src = dst;
+        dst = t;
     }
     *result = src;
 }
@@ -335,26 +482,18 @@ namespace {
 
 // Runs the LSD passes so that the last pass lands in `out`; the first pass reads `in` and never writes it.
 void sort_into(const u64 *in, u64 *out, u64 *alt, u64 n, int key_bits, void *tmp, cudaStream_t s) {
-    int passes = 0;
-    for (int shift = 0; shift < key_bits; shift += 8) passes++;
+    int width[4];
+    const int passes = rs_passes(key_bits, width);
     if (n <= 1 || passes == 0) {
         if (n) cudaMemcpyAsync(out, in, n * sizeof(u64), cudaMemcpyDeviceToDevice, s);
         return;
     }
-    const u32 nblocks = u32((n + RS_TILE - 1) / RS_TILE);
-    const u64 hist_n = u64(nblocks) * 256;
-    u32 *hist = reinterpret_cast<u32 *>(tmp);
-    u32 *offs = hist + hist_n + 1;
-    void *stmp = offs + hist_n + 1;
+    const RsPlan plan = rs_plan(n);
     const u64 *src = in;
-    int p = 0;
-    for (int shift = 0; shift < key_bits; shift += 8, p++) {
+    for (int p = 0, shift = 0; p < passes; shift += width[p], p++) {
         // pass p writes `out` when the number of passes left (passes - p) is odd
         u64 *dst = ((passes - p) % 2 == 1) ? out : alt;
-        k_rs_hist<<<nblocks, RS_THREADS, 0, s>>>(src, n, shift, key_bits, hist, nblocks);
-        scan_rec(hist, offs, hist_n, reinterpret_cast<u32 *>(stmp), s);
-        k_rs_scatter<<<nblocks, RS_THREADS, 0, s>>>(src, n, shift, key_bits, offs, nblocks, dst);
-        g_kernel_launches += 2;
+        rs_pass(src, dst, n, shift, width[p], plan, tmp, s);
         src = dst;
     }
 }
