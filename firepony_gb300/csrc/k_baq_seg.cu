@@ -631,6 +631,10 @@ __global__ void __launch_bounds__(SEG_THREADS, SEG_BLOCKS_PER_SM)
                     } else if (!(thi < 100.f && flo == fhi) && !(tlo >= 101.5f)) {
                         amb |= 1;
                     }
+                    // bit 8: the state is undecided, but every candidate's MAP quality is MIN_BASE_QUAL (a rival
+                    // within the bound keeps the best posterior near 1/2, so t < 5 whichever term the exact
+                    // computation picks)
+                    if ((amb & 2) && thi < 4.9f) amb |= 8;
                 }
                 w.baq_q[qi] = u8(qv);
                 w.baq_state[qi] = state;

@@ -633,6 +633,8 @@ __global__ void __launch_bounds__(TPR_THREADS) k_baq_tpr(DevBatch b, DevRef dref
                     } else if (!(hi < 100.f && flo == fhi) && !(lo >= 101.5f)) {
                         amb |= 1;
                     }
+                    // bit 8: undecided state, every candidate's MAP quality MIN_BASE_QUAL (t < 5 for all)
+                    if ((amb & 2) && hi < 4.9f) amb |= 8;
                 }
                 w.baq_q[qi] = u8(qv);
                 w.baq_state[qi] = state;

@@ -653,7 +653,9 @@ __global__ void __launch_bounds__(PREP_WARPS * 32) k_prep(DevBatch b, DevRef ref
 // original quality per I base. In FP32 mode (exact == 0) the HMM outputs can be undecided (baq_amb); if a
 // capped value depends on one (an undecided quality of a base whose state is the match at its expected
 // position, or an undecided state whose candidates do not all give MIN_BASE_QUAL), the read goes to the
-// escalation list and the exact replay's capping rewrites its values.
+// escalation list and the exact replay's capping rewrites its values. A state left undecided by a rival
+// within the bound (baq_amb bit 2) caps at MIN_BASE_QUAL whichever candidate wins whenever the kernel also
+// proved every candidate's MAP quality to be MIN_BASE_QUAL (bit 8) and the original quality is at least that.
 __global__ void __launch_bounds__(64) k_cap(DevBatch b, BatchWork w, const u32 *list, const u32 *count, int exact) {
     constexpr u32 FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -723,7 +725,10 @@ __global__ void __launch_bounds__(64) k_cap(DevBatch b, BatchWork w, const u32 *
                 const bool at_expected = (state & 3) == 0 && (state >> 2) == expectedPos;
                 if (!exact) {
                     const u8 amb = w.baq_amb[qs + rb];
-                    if (amb & 4) {
+                    if ((amb & 8) && oq >= MIN_BASE_QUAL) {
+                        // undecided state whose candidates all have MAP quality MIN_BASE_QUAL: min(bq, oq) at
+                        // the expected match and MIN_BASE_QUAL elsewhere are the same value
+                    } else if (amb & 4) {
                         escalate = true;
                         by_state = true;
                     } else if (amb & 2) {

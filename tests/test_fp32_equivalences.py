@@ -45,3 +45,30 @@ def test_fp32_baq_range_arguments():
     assert float(flush) == 3.3087224502121107e-24
     # posterior terms of two kept values may underflow: 2^-150 each at most, far below a row sum >= 2^0
     assert 2 * 63 * 2.0 ** -150 < 2.0 ** -24
+
+
+def test_tied_map_states_cap_at_min_base_qual():
+    """A base whose MAP state is undecided (a rival term within the certified bound of the maximum) keeps the
+    best posterior at or below about 1/2, so the reference's MAP quality (device/baq.cu:673: (int)(-4.343 *
+    log(1 - max) + .499), clamped to [MIN_BASE_QUAL, 99]) is MIN_BASE_QUAL = 4 whichever term wins; the FP32
+    kernels additionally require the certified upper end of t below 4.9. The capping step
+    (device/baq.cu:895-909) then gives min(4, oq) at the expected match and 4 elsewhere: one value when oq >= 4."""
+    min_base_qual = 4
+
+    def map_quality(p_max):
+        k = np.trunc(-4.343 * np.log(1.0 - p_max) + 0.499).astype(np.int64)
+        return np.where(k > 100, 99, np.where(k < min_base_qual, min_base_qual, k))
+
+    rel_state = 1e-3  # far wider than any kernel's state bound
+    # posterior of the best of two terms within rel_state of each other, any remaining mass elsewhere
+    p = np.linspace(0.0, 1.0 / (2.0 - rel_state), 200_001)
+    assert (map_quality(p) == min_base_qual).all()
+    # a candidate's t exceeds the certified upper end by far less than 0.05 (a few relative bounds of about
+    # 1e-4); t up to 4.9 + 0.05 still floors to 4
+    t_hi = np.float32(4.9)
+    p_at = 1.0 - np.exp((0.499 - float(t_hi) - 0.05) / 4.343)
+    assert map_quality(np.array([p_at]))[0] == min_base_qual
+    oq = np.arange(0, 94)
+    at_expected = np.minimum(min_base_qual, oq)
+    elsewhere = np.full_like(oq, min_base_qual)
+    assert ((at_expected == elsewhere) == (oq >= min_base_qual)).all()
