@@ -743,8 +743,7 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
             if (c == 0)
                 launch_baq_seg(b, eng->ref, w, list, w.counters + c, n_cls[c], ctr, scr, scr_bytes, max_q, cs);
             else
-                launch_baq_tpr(b, eng->ref, w, list, w.counters + c, n_cls[c], c, false, ctr, scr, scr_bytes, max_q, 32,
-                               cs);
+                launch_baq_wide16(b, eng->ref, w, list, w.counters + c, n_cls[c], ctr, scr, scr_bytes, max_q, cs);
             if (c == 0) { cudaEventRecord(eng->ev[11], cs); timed_main = true; }
             launch_cap(b, w, list, w.counters + c, 0, cs, n_cls[c]);
         };

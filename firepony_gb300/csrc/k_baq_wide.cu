@@ -49,7 +49,7 @@ __device__ __forceinline__ void flush(float &v, float &c) {
     }
 }
 
-// sums / maxima over the G lanes of a group (every lane gets the result)
+// sums / maxima over the G lanes of a group (every lane gets the result; every lane of the warp must call them)
 template <int G> __device__ __forceinline__ float gsum(float v) {
 #pragma unroll
     for (int o = G / 2; o >= 1; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
@@ -70,12 +70,6 @@ template <int G> __device__ __forceinline__ u32 gminu(u32 v) {
     for (int o = G / 2; o >= 1; o >>= 1) v = min(v, __shfl_xor_sync(FULL, v, o));
     return v;
 }
-template <int G> __device__ __forceinline__ bool gany(bool v) {
-    u32 x = v ? 1u : 0u;
-#pragma unroll
-    for (int o = G / 2; o >= 1; o >>= 1) x |= __shfl_xor_sync(FULL, x, o);
-    return x != 0;
-}
 
 // MAP quality bounds as in k_baq_tpr: the capped quality of t, saturating like the reference's CUDA build
 __device__ __forceinline__ int capped_q(float tt) {
@@ -89,7 +83,7 @@ __device__ __forceinline__ int capped_q(float tt) {
 template <int G, int NS>
 __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref, BatchWork w, const u32 *list,
                                                          const u32 *count, u32 *work_ctr, float *scratch,
-                                                         u32 max_q) {
+                                                         u32 max_q, int min_bw) {
     constexpr int WC = G * NS;          // band slots per read
     constexpr int GPW = 32 / G;         // reads (groups) per warp
     constexpr int WPB = WD_THREADS / 32;
@@ -128,6 +122,7 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
         bool has = li < n_list;
         const u32 r = has ? list[li] : 0;
         if (has && 2 * int(w.bw[r]) + 1 > WC) has = false;  // left to the thread-per-read FP64 kernel
+        if (has && int(w.bw[r]) < min_bw) has = false;       // a narrower kernel of the same class takes it
 
         // ---- setup (device/baq.cu:247-334), identical for the lanes of a group ----
         int qL = 0, refLen = 0, bmLen = 1, bw = 0;
@@ -460,7 +455,9 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
             const float thr = mx * (1.0f - rel_state) - 2.0f * abs_err;
             // an undecided state records its rival when there is exactly one
             u32 rivals = 0, alt = 0xFFFFFFFFu;
-            if (gany<G>(act && valid && second >= thr)) {
+            // (a warp-wide vote: the group sums below are full-warp shuffles, so every lane must take this branch
+            // when any group does; a group without a rival counts none)
+            if (__any_sync(FULL, act && valid && second >= thr)) {
                 u32 c = 0, a = 0xFFFFFFFFu;
 #pragma unroll
                 for (int j = 0; j < NS; j++) {
@@ -545,7 +542,7 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
 
 template <int G, int NS>
 void launch_w(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
-              u32 max_reads, u32 *ctr, float *scratch, u64 scratch_elems, u32 max_q, cudaStream_t s) {
+              u32 max_reads, u32 *ctr, float *scratch, u64 scratch_elems, u32 max_q, cudaStream_t s, int min_bw = 0) {
     constexpr int WC = G * NS, GPW = 32 / G;
     const u64 per_group = (u64(max_q) + 2) * (2 * WC + 1);
     const u64 groups = scratch_elems / per_group;
@@ -556,7 +553,7 @@ void launch_w(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u3
     if (blocks > 152 * 8) blocks = 152 * 8;
     if (blocks == 0) return;
     cudaMemsetAsync(ctr, 0, sizeof(u32), s);
-    k_baq_wide<G, NS><<<u32(blocks), WD_THREADS, 0, s>>>(b, ref, w, list, count, ctr, scratch, max_q);
+    k_baq_wide<G, NS><<<u32(blocks), WD_THREADS, 0, s>>>(b, ref, w, list, count, ctr, scratch, max_q, min_bw);
     g_kernel_launches++;
 }
 
@@ -568,19 +565,32 @@ void baq_wide_set_constants(const HmmConst &c) {
 }
 
 u64 baq_wide_scratch_bytes(u32 reads, u32 max_q) {
-    // whole blocks (the launch sizes its grid by the groups the scratch holds; fewer than a block launches none)
-    constexpr u64 per_block = WD_THREADS / 32;  // groups per block (one read per warp)
-    const u64 per_group = (u64(max_q) + 2) * (2 * 64 + 1) * sizeof(float);
+    // whole blocks of the 32 x 2 kernel (the launch sizes its grid by the groups the scratch holds; fewer than a
+    // block launches none), and at least one block of the 16 x 3 kernel (two groups per warp)
+    constexpr u64 per_block = WD_THREADS / 32;  // groups per block of the 32 x 2 kernel (one read per warp)
+    const u64 rows = u64(max_q) + 2;
+    const u64 per_group = rows * (2 * 64 + 1) * sizeof(float);
     u64 groups = std::min<u64>(std::max<u32>(reads, 1), 152ull * 8 * per_block);
     groups = (groups + per_block - 1) / per_block * per_block;
-    return per_group * groups;
+    const u64 block_16x3 = rows * (2 * 48 + 1) * sizeof(float) * (2 * per_block);
+    return std::max<u64>(per_group * groups, block_16x3);
 }
 
 void launch_baq_wide(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
                      u32 max_reads, u32 *ctr, void *scratch, u64 scratch_bytes, u32 max_q, cudaStream_t s) {
     if (!max_reads) return;
-    // bands up to bw 31 (63 cells): 32 lanes x 2 slots, a read per warp
-    launch_w<32, 2>(b, ref, w, list, count, max_reads, ctr, (float *)scratch, scratch_bytes / 4, max_q, s);
+    // bands up to bw 23 (47 cells): 16 lanes x 3 slots, two reads per warp; bw 24..31 (63 cells): 32 lanes x 2
+    // slots, a read per warp. Each kernel takes its share of the list and skips the other's reads; the two share
+    // the scratch and the work counters, so they run one after the other.
+    launch_w<16, 3>(b, ref, w, list, count, max_reads, ctr, (float *)scratch, scratch_bytes / 4, max_q, s);
+    launch_w<32, 2>(b, ref, w, list, count, max_reads, ctr, (float *)scratch, scratch_bytes / 4, max_q, s, 24);
+}
+
+void launch_baq_wide16(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
+                       u32 max_reads, u32 *ctr, void *scratch, u64 scratch_bytes, u32 max_q, cudaStream_t s) {
+    if (!max_reads) return;
+    // band class 1 (bw <= 15, at most 31 cells): 16 lanes x 2 slots, two reads per warp
+    launch_w<16, 2>(b, ref, w, list, count, max_reads, ctr, (float *)scratch, scratch_bytes / 4, max_q, s);
 }
 
 }  // namespace fpg

@@ -144,17 +144,34 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_count(const u64 *in, u64 n, i
     const u64 k0 = u64(c) * tpc * RS_TILE;
     const u64 k1 = k0 + u64(tpc) * RS_TILE < n ? k0 + u64(tpc) * RS_TILE : n;
     const u64 len = k1 - k0;
-    const u64 a = k0 + len * part / RS_COUNT_SPLIT, b = k0 + len * (part + 1) / RS_COUNT_SPLIT;
-    constexpr int U = 8;
-    u64 i = a + threadIdx.x;
-    for (; i + u64(U - 1) * RS_THREADS < b; i += u64(U) * RS_THREADS) {
-        u64 x[U];
-#pragma unroll
-        for (int j = 0; j < U; j++) x[j] = in[i + u64(j) * RS_THREADS];
-#pragma unroll
-        for (int j = 0; j < U; j++) atomicAdd(&h[warp][digit_of(x[j], shift, mask)], 1u);
+    u64 a = k0 + len * part / RS_COUNT_SPLIT;
+    const u64 b = k0 + len * (part + 1) / RS_COUNT_SPLIT;
+    // pairs of entries as 16-byte loads from the first 16-byte boundary; one entry before it and one after the
+    // last pair are counted by thread 0
+    if ((reinterpret_cast<uintptr_t>(in + a) & 15) && a < b) {
+        if (threadIdx.x == 0) atomicAdd(&h[warp][digit_of(in[a], shift, mask)], 1u);
+        a++;
     }
-    for (; i < b; i += RS_THREADS) atomicAdd(&h[warp][digit_of(in[i], shift, mask)], 1u);
+    const u64 np = (b - a) / 2;
+    const ulonglong2 *in2 = reinterpret_cast<const ulonglong2 *>(in + a);
+    constexpr int U = 4;
+    u64 i = threadIdx.x;
+    for (; i + u64(U - 1) * RS_THREADS < np; i += u64(U) * RS_THREADS) {
+        ulonglong2 x[U];
+#pragma unroll
+        for (int j = 0; j < U; j++) x[j] = in2[i + u64(j) * RS_THREADS];
+#pragma unroll
+        for (int j = 0; j < U; j++) {
+            atomicAdd(&h[warp][digit_of(x[j].x, shift, mask)], 1u);
+            atomicAdd(&h[warp][digit_of(x[j].y, shift, mask)], 1u);
+        }
+    }
+    for (; i < np; i += RS_THREADS) {
+        const ulonglong2 x = in2[i];
+        atomicAdd(&h[warp][digit_of(x.x, shift, mask)], 1u);
+        atomicAdd(&h[warp][digit_of(x.y, shift, mask)], 1u);
+    }
+    if (a + 2 * np < b && threadIdx.x == 0) atomicAdd(&h[warp][digit_of(in[b - 1], shift, mask)], 1u);
     __syncthreads();
     for (int d = threadIdx.x; d < D; d += RS_THREADS) {
         u32 s = 0;
@@ -227,7 +244,7 @@ __global__ void __launch_bounds__(RS_THREADS, RS_CTAS_PER_SM)
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             const int d = 4 * threadIdx.x + k;
-            if (d < D) S.next[d] = p + colpre[u64(blockIdx.x) * D + d];
+            S.next[d] = d < D ? p + colpre[u64(blockIdx.x) * D + d] : 0u;
             p += t4[k];
         }
     }
@@ -276,38 +293,32 @@ __global__ void __launch_bounds__(RS_THREADS, RS_CTAS_PER_SM)
         }
         __syncthreads();
         {
-            // per digit (thread t: digits 4t..4t+3): the warps' counts become their first slots within the
-            // digit, the tile's digit counts are scanned into the digits' first slots in the tile
-            u32 tc[4], sum = 0;
+            // per digit (thread t: digits 4t..4t+3, one 8-byte word of counts per warp): the warps' counts become
+            // their first slots within the digit, the tile's digit counts are scanned into the digits' first
+            // slots in the tile. Two 16-bit counts per word add without carries (a tile holds 4096 keys).
+            const int d0 = 4 * threadIdx.x;
+            uint2 c[RS_WARPS];
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
-                const int d = 4 * threadIdx.x + k;
-                u32 acc = 0;
-                if (d < D) {
+            for (int w = 0; w < RS_WARPS; w++) c[w] = *reinterpret_cast<const uint2 *>(&S.cnt[w][d0]);
+            uint2 acc = make_uint2(0, 0);
 #pragma unroll
-                    for (int w = 0; w < RS_WARPS; w++) {
-                        const u32 c = S.cnt[w][d];
-                        S.cnt[w][d] = u16(acc);
-                        acc += c;
-                    }
-                }
-                tc[k] = acc;
-                sum += acc;
+            for (int w = 0; w < RS_WARPS; w++) {
+                const uint2 x = c[w];
+                c[w] = acc;
+                acc.x += x.x;
+                acc.y += x.y;
             }
+            const u32 tc0 = acc.x & 0xFFFFu, tc1 = acc.x >> 16, tc2 = acc.y & 0xFFFFu, tc3 = acc.y >> 16;
             u32 total;
-            u32 start = block_exclusive_scan(sum, &total);
+            const u32 s0 = block_exclusive_scan(tc0 + tc1 + tc2 + tc3, &total);
+            const u32 s1 = s0 + tc0, s2 = s1 + tc1, s3 = s2 + tc2;
+            const uint2 add = make_uint2(s0 | (s1 << 16), s2 | (s3 << 16));
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
-                const int d = 4 * threadIdx.x + k;
-                if (d < D) {
-#pragma unroll
-                    for (int w = 0; w < RS_WARPS; w++) S.cnt[w][d] = u16(S.cnt[w][d] + start);
-                    const u32 nd = S.next[d];
-                    S.off[d] = nd - start;
-                    S.next[d] = nd + tc[k];
-                }
-                start += tc[k];
-            }
+            for (int w = 0; w < RS_WARPS; w++)
+                *reinterpret_cast<uint2 *>(&S.cnt[w][d0]) = make_uint2(c[w].x + add.x, c[w].y + add.y);
+            const uint4 nx = *reinterpret_cast<const uint4 *>(&S.next[d0]);
+            *reinterpret_cast<uint4 *>(&S.off[d0]) = make_uint4(nx.x - s0, nx.y - s1, nx.z - s2, nx.w - s3);
+            *reinterpret_cast<uint4 *>(&S.next[d0]) = make_uint4(nx.x + tc0, nx.y + tc1, nx.z + tc2, nx.w + tc3);
         }
         __syncthreads();
 #pragma unroll
@@ -318,9 +329,21 @@ __global__ void __launch_bounds__(RS_THREADS, RS_CTAS_PER_SM)
             }
         }
         __syncthreads();
-        for (u32 p = threadIdx.x; p < tile_n; p += RS_THREADS) {
-            const u64 key = S.buf[p];
-            out[u32(S.off[digit_of(key, shift, mask)] + p)] = key;
+        if (tile_n == u32(RS_TILE)) {
+            // a whole tile: every load issued before the dependent lookups and stores
+            u64 kk[RS_ROUNDS];
+            u32 oo[RS_ROUNDS];
+#pragma unroll
+            for (int j = 0; j < RS_ROUNDS; j++) kk[j] = S.buf[threadIdx.x + j * RS_THREADS];
+#pragma unroll
+            for (int j = 0; j < RS_ROUNDS; j++) oo[j] = S.off[digit_of(kk[j], shift, mask)];
+#pragma unroll
+            for (int j = 0; j < RS_ROUNDS; j++) out[u32(oo[j] + threadIdx.x + j * RS_THREADS)] = kk[j];
+        } else {
+            for (u32 p = threadIdx.x; p < tile_n; p += RS_THREADS) {
+                const u64 key = S.buf[p];
+                out[u32(S.off[digit_of(key, shift, mask)] + p)] = key;
+            }
         }
     }
 }
