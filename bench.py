@@ -267,6 +267,7 @@ def run_batched(args):
         out["baq_reads_by_band"] = st["baq_reads_by_band"]
         out["baq_escalated_by_band"] = st["baq_escalated_by_band"]
         out["baq_fp64_escalated_reads"] = st["baq_fp64_escalated_reads"]
+        out["baq_escalated_by_cause"] = st["baq_escalated_by_cause"]
         # bounded sample: per batch / coalesced / plain FP64 coalesced, identical tables
         sample = pinned[:args.batched_sample]
         sreads = int(sum(b.num_reads for b in sample))
