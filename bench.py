@@ -268,6 +268,7 @@ def run_batched(args):
         out["baq_escalated_by_band"] = st["baq_escalated_by_band"]
         out["baq_fp64_escalated_reads"] = st["baq_fp64_escalated_reads"]
         out["baq_escalated_by_cause"] = st["baq_escalated_by_cause"]
+        out["baq_escalated_undecided_rows"] = st["baq_escalated_undecided_rows"]
         # bounded sample: per batch / coalesced / plain FP64 coalesced, identical tables
         sample = pinned[:args.batched_sample]
         sreads = int(sum(b.num_reads for b in sample))
@@ -905,6 +906,7 @@ def main():
                 "baq_reads_by_band": res["stats"]["baq_reads_by_band"],
                 "baq_escalated_by_band": res["stats"]["baq_escalated_by_band"],
                 "baq_escalated_by_cause": res["stats"]["baq_escalated_by_cause"],
+                "baq_escalated_undecided_rows": res["stats"]["baq_escalated_undecided_rows"],
                 "baq_path_ms": [round(v, 3) for v in res["stats"]["baq_path_ms"]],
                 "e2e_tables_identical": bool(res["same"])}
         print(json.dumps(line))

@@ -46,7 +46,8 @@ class FpStats(C.Structure):
                 ("baq_reads_by_band", C.c_uint64 * 3), ("baq_escalated_by_band", C.c_uint64 * 2),
                 ("baq_escalated_by_cause", C.c_uint64 * 2),
                 ("baq_band_cells", C.c_uint64 * 3), ("baq_main_launches", C.c_uint64),
-                ("baq_main_ms", C.c_double), ("baq_path_ms", C.c_double * 4)]
+                ("baq_main_ms", C.c_double), ("baq_path_ms", C.c_double * 4),
+                ("baq_escalated_undecided_rows", C.c_uint64)]
 
 
 class FpPrecisionStats(C.Structure):

@@ -893,7 +893,7 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
     cudaEventRecord(eng->ev[6], st);
     u32 dev_err = 0;
     unsigned long long cells[3] = {0, 0, 0};
-    u32 cause[2] = {0, 0};
+    u32 cause[4] = {0, 0, 0, 0};  // counters 22..25: state, quality, (class-1 replay work counter), unbounded rows
     CK(cudaMemcpyAsync(cells, w.counters + 16, sizeof(cells), cudaMemcpyDeviceToHost, st), "D2H");
     CK(cudaMemcpyAsync(cause, w.counters + 22, sizeof(cause), cudaMemcpyDeviceToHost, st), "D2H");
     CK(cudaMemcpyAsync(cnt, w.counters, sizeof(cnt), cudaMemcpyDeviceToHost, st), "D2H");
@@ -918,6 +918,7 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
     }
     eng->stats.baq_escalated_by_cause[0] += cause[0];
     eng->stats.baq_escalated_by_cause[1] += cause[1];
+    eng->stats.baq_escalated_undecided_rows += cause[3];
     eng->stats.baq_escalated_by_band[0] += tail[1];
     eng->stats.baq_escalated_by_band[1] += u64(esc1) + esc2;
     if (timed_paths) {

@@ -699,7 +699,7 @@ __global__ void __launch_bounds__(64) k_cap(DevBatch b, BatchWork w, const u32 *
         // walk does not depend on the HMM) before anything reads them.
         u32 end = n;
         u32 refI_c = 0, numD_c = 0, readI_c = 0;
-        bool escalate = false, by_state = false;
+        bool escalate = false, by_state = false, unbounded = false;
         for (u32 c = baq_start; c < end; c += 32) {
             const u32 i = c + lane;
             const u32 rcv = i < end ? rc[i] : u32(U16_NONE);
@@ -725,6 +725,7 @@ __global__ void __launch_bounds__(64) k_cap(DevBatch b, BatchWork w, const u32 *
                 const bool at_expected = (state & 3) == 0 && (state >> 2) == expectedPos;
                 if (!exact) {
                     const u8 amb = w.baq_amb[qs + rb];
+                    unbounded |= amb == 7;  // a row the FP32 pass left wholly undecided
                     if ((amb & 8) && oq >= MIN_BASE_QUAL) {
                         // undecided state whose candidates all have MAP quality MIN_BASE_QUAL: min(bq, oq) at
                         // the expected match and MIN_BASE_QUAL elsewhere are the same value
@@ -769,6 +770,8 @@ __global__ void __launch_bounds__(64) k_cap(DevBatch b, BatchWork w, const u32 *
             // escalation cause: some MAP state undecided, or only qualities undecided
             const bool st = __any_sync(FULL, by_state);
             if (lane == 0) atomicAdd(&w.counters[st ? 22 : 23], 1u);
+            const bool ub = __any_sync(FULL, unbounded);
+            if (lane == 0 && ub) atomicAdd(&w.counters[25], 1u);
         }
     }
 }

@@ -144,6 +144,9 @@ typedef struct {
     double   baq_path_ms[4];             /* FP32 mode, device time from the BAQ stage start to the end of: the
                                             class-0 FP32 kernel + capping, the class-0 replay, the class-1
                                             FP32 kernel + capping, the class-1 replay */
+    uint64_t baq_escalated_undecided_rows; /* FP32 mode: of the replays with an undecided MAP state, those
+                                            holding rows the FP32 pass could not bound at all (the band-class-0
+                                            underflow guard, a row without a usable sum, a quality above 93) */
 } fp_stats;
 
 /* FP32 vs FP64 per BAQ read (FP_FLAG_PRECISION_TRACE), accumulated since creation or reset. t is the MAP
