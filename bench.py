@@ -29,9 +29,11 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_baq_tpr<float,15> launch on a 1M-read batch of the
-# workload, from an ncu capture of this bench (`--set full -k regex:k_baq_tpr -s 1 -c 1` on one 1M-read batch)
-TRAFFIC_BYTES_PER_LAUNCH = 34.93e9
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_baq_seg launch per band-class-0 read, from an ncu capture
+# of a 100k-read batch of the workload (78,770 class-0 reads, 921.6 MB; `--batch-reads 100000 ... ncu --set full
+# -k regex:k_baq_seg -s 1 -c 1`); the checkpoint scratch traffic is per read, so a launch's traffic scales with
+# its reads
+TRAFFIC_BYTES_PER_READ = 11700.0
 METRIC = "reads/s on 1 GB300, batched vs plain, bit-exact recal table; p50/p99 job latency"
 WORKLOAD = ("precision_20M_151bp_pe: paired-end 151 bp reads, 8 read groups (quality offsets -3..+3), "
             "5 contigs / 50 Mbp, 50k known SNPs + 5k known indels, 2% indel reads, 1% substitutions rising to 3'")
@@ -755,9 +757,8 @@ def fp32_peak():
 
 
 def roofline(res, args, peak32):
-    """Roofline of the dominant kernel, the band-class-0 BAQ HMM (k_baq_tpr<float, 15>: bandwidth 7, FP32 with
-    certified bounds), timed by the engine with CUDA events around each of its launches inside the timed
-    region. Algorithmic bytes per read of that class (L = mean HMM query length): L/2 packed bases + L
+    """Roofline of the dominant kernel, the band-class-0 BAQ HMM (k_baq_seg: bandwidth 7, FP32 with certified
+    bounds), timed by the engine with CUDA events around each of its launches inside the timed region. Algorithmic bytes per read of that class (L = mean HMM query length): L/2 packed bases + L
     qualities + (L + 6)/2 packed reference window + L BAQ qualities + 4 L MAP states written. Algorithmic
     work: 41 FP32 operations per band cell (forward 19, backward 16, MAP 6), band cells counted exactly per
     read by the engine. The HMM is an FP32 SIMT recurrence, so the compute figure is the binding one; the
@@ -784,8 +785,8 @@ def roofline(res, args, peak32):
     measured = max(peak32.get("scalar_fma_tflops", 0.0), peak32.get("packed_fma2_tflops", 0.0))
     f32 = measured if measured > 0 else nominal
     return {"bound": "hbm", "achieved": round(achieved_gbs, 2), "peak": hbm, "unit": "GB/s",
-            "frac": round(achieved_gbs / hbm, 5), "traffic": TRAFFIC_BYTES_PER_LAUNCH,
-            "kernel": "k_baq_tpr<float,15> (BAQ HMM, band class 0)",
+            "frac": round(achieved_gbs / hbm, 5), "traffic": round(TRAFFIC_BYTES_PER_READ * reads),
+            "kernel": "k_baq_seg (BAQ HMM, band class 0)",
             "launch_ms": round(ms, 3), "reads_per_launch": int(reads), "band_cells_per_launch": int(cells),
             "peak_source": "measured" if peaks else "fallback",
             "compute": {"unit": "TFLOP/s", "achieved": round(tops, 3), "peak": round(f32, 2),

@@ -12,7 +12,9 @@ Two shapes of the per-batch path are chosen at run time (fp_options):
 `autotune` times every combination on the sample batches (a warm-up pass, then one timed pass from the first
 submit to the finished tables) and requires every candidate's tables to equal the first one's: a shape never
 changes results, so a difference is an error, not a trade-off. The fastest combination is returned as
-Engine keyword arguments.
+Engine keyword arguments. Coalescing targets at or above the sample's read count all gather the whole sample
+into one device batch, so the sample cannot tell them apart; when the fastest is one of them, the largest such
+target is returned, which on the full workload makes the fewest and largest device batches.
 
     python -m firepony_gb300.autotune --workload batched_uneven --batches 16 --out tuned.json
     Engine(num_read_groups=16, **json.load(open("tuned.json"))["best"])
@@ -72,8 +74,10 @@ def autotune(reference, batches, num_read_groups: int, replay_choices=REPLAY_CHO
             results.append(row)
             if best is None or dt < best["seconds"]:
                 best = row
-    return {"best": {"replay_reads_per_warp": best["replay_reads_per_warp"],
-                     "coalesce_reads": best["coalesce_reads"]},
+    co_best = best["coalesce_reads"]
+    if co_best >= reads:
+        co_best = max(co for co in coalesce_choices if co >= reads)
+    return {"best": {"replay_reads_per_warp": best["replay_reads_per_warp"], "coalesce_reads": co_best},
             "results": results, "reads": reads}
 
 

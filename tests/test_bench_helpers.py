@@ -44,3 +44,24 @@ def test_cpu_baseline_times_the_oracle_on_prebuilt_ranges():
     assert set(out["stages"]["share"]) == set(STAGES)
     assert abs(sum(out["stages"]["share"].values()) - 1.0) < 1e-3
     assert out["stages"]["thread_s"]["baq_hmm"] > 0
+
+
+def test_autotune_takes_the_largest_target_the_sample_cannot_tell_apart(monkeypatch):
+    """Coalescing targets at or above the sample's read count all make one device batch of the sample; when the
+    fastest candidate is one of them, the largest is returned."""
+    import numpy as np
+    from firepony_gb300 import autotune as at
+
+    class B:
+        num_reads = 1000
+
+    tables = {0: {"keys": np.arange(3)}}
+    times = {(0, 0): 3.0, (0, 500): 2.0, (0, 2000): 1.0, (0, 8000): 1.1, (4, 0): 5.0, (4, 500): 5.0,
+             (4, 2000): 5.0, (4, 8000): 5.0}
+    monkeypatch.setattr(at, "time_config", lambda ref, batches, n_rg, rpw, co, device=0: (times[(rpw, co)], tables))
+    res = at.autotune(None, [B(), B()], 1, replay_choices=(0, 4), coalesce_choices=(0, 500, 2000, 8000))
+    assert res["reads"] == 2000
+    assert res["best"] == {"replay_reads_per_warp": 0, "coalesce_reads": 8000}
+    times[(0, 500)] = 0.5  # a target below the sample's size that wins is kept as is
+    res = at.autotune(None, [B(), B()], 1, replay_choices=(0, 4), coalesce_choices=(0, 500, 2000, 8000))
+    assert res["best"]["coalesce_reads"] == 500
