@@ -307,7 +307,10 @@ __global__ void __launch_bounds__(COV_WARPS * 32) k_cov(DevBatch b, BatchWork w,
                         if (run_end) atomicAdd(d + (neg ? a : a + 1), neg ? 1 : -1);
                     }
                 }
-                agg_add(t.stage, kx0, g && vxm, lane);
+                // context M keys spread over (read group, quality, 2-mer): one plain atomic per lane costs fewer issue
+                // slots than a match-based aggregation (the quality and context I/D keys below collide far more
+                // often within a warp and keep theirs)
+                if (g && vxm) atomicAdd(&t.stage[kx0], 1u);
                 if (hw_n) {
                     if (g && vxi) atomicAdd(&hist_x[rg * 80 + context_rank(ci)], 1u);
                 } else {
