@@ -773,21 +773,20 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
             run_fp32(0, st, eng->s32.p, budget, w.counters + 8);
             cudaEventRecord(eng->ev[14], st);
         }
-        // bands wider than 15: FP32 with certified bounds, the band across a warp's lanes, for bw <= 31 (its
+        // bands wider than 15: FP32 with certified bounds, the band across a warp's lanes, for bw <= 63 (its
         // undecided reads join the replays); exact FP64 for wider ones (each kernel skips the others' reads; the
         // FP64 results are final, so the capping step finds them decided)
         if (n_cls[2]) {
             const u32 *list2 = w.baq_list + 2ull * R;
-            // (the exact kernels below and the class-2 replay reuse the buffer)
-            const u64 exact_bytes = std::max(baq_exact_block_scratch_bytes(2, max_q),
-                                             bw_max[2] > 31 ? baq_exact_block_scratch_bytes(3, max_q) : 0);
-            CK(eng->s32w.ensure(std::max(baq_wide_scratch_bytes(n_cls[2], max_q), exact_bytes)), "BAQ scratch");
+            // (the class-2 replay reuses the buffer)
+            CK(eng->s32w.ensure(std::max(baq_wide_scratch_bytes(n_cls[2], max_q), baq_exact_block_scratch_bytes(2, max_q))),
+               "BAQ scratch");
             launch_baq_wide(b, eng->ref, w, list2, w.counters + 2, n_cls[2], w.counters + 26, eng->s32w.p,
                             eng->s32w.cap, max_q, st);
-            // bw 32..63: exact FP64 across a warp's lanes, every row; wider: the thread-per-read FP64 kernel
+            // bw 32..63: the same with 32 lanes x 4 slots; wider: the thread-per-read FP64 kernel
             if (bw_max[2] > 31)
-                launch_baq_exact(b, eng->ref, w, list2, w.counters + 2, n_cls[2], 3, w.counters + 29, eng->s32w.p,
-                                 eng->s32w.cap, max_q, true, st);
+                launch_baq_wide64(b, eng->ref, w, list2, w.counters + 2, n_cls[2], w.counters + 29, eng->s32w.p,
+                                  eng->s32w.cap, max_q, st);
             if (bw_max[2] > 63 && (s = run_fp64(list2, w.counters + 2, n_cls[2], bw_max[2], 64, false)) != FP_OK)
                 return s;
             launch_cap(b, w, list2, w.counters + 2, 0, st, n_cls[2]);

@@ -432,8 +432,7 @@ u64 baq_exact_block_scratch_bytes(int band_class, u32 max_q) {
     auto block = [&](int wc, int gpw) { return u64(gpw) * (EX_THREADS / 32) * (u64(max_q) + 2) * (2 * wc + 3) * 8; };
     if (band_class == 0) return block(16, 4);
     if (band_class == 1) return block(32, 2);
-    if (band_class == 2) return std::max(block(48, 2), block(64, 1));
-    return block(128, 1);
+    return std::max(std::max(block(48, 2), block(64, 1)), block(128, 1));
 }
 
 void baq_exact_set_constants(const HmmConst &c) {
@@ -445,22 +444,19 @@ void launch_baq_exact(const DevBatch &b, const DevRef &ref, const BatchWork &w, 
                       u32 max_reads, int band_class, u32 *ctr, void *scratch, u64 scratch_bytes, u32 max_q,
                       bool all_rows, cudaStream_t s) {
     if (!max_reads) return;
-    // band_class 3: the reads of the class-2 list with bw 32..63 (every row; the FP32 kernel skips them)
     // band class 0 (bw <= 7, 15 slots): 8 lanes x 2 slots, 4 reads per warp; class 1 (bw <= 15, 31 slots):
     // 16 lanes x 2 slots, 2 reads per warp; wider bands: 16 lanes x 3 slots (bw <= 23, 2 reads per warp), then
-    // 32 lanes x 2 slots for the rest up to bw 31 (a read per warp; the second launch reuses the work counter
-    // after the first finishes on the same stream)
+    // 32 lanes x 2 slots up to bw 31 and 32 lanes x 4 slots up to bw 63 (a read per warp; each later launch reuses
+    // the work counter after the earlier one finishes on the same stream)
     double *d = (double *)scratch;
     const int full = all_rows ? 1 : 0;
     if (band_class == 0) {
         launch_g<8, 2>(b, ref, w, list, count, max_reads, ctr, d, scratch_bytes / 8, max_q, full, s);
     } else if (band_class == 1) {
         launch_g<16, 2>(b, ref, w, list, count, max_reads, ctr, d, scratch_bytes / 8, max_q, full, s);
-    } else if (band_class == 2) {
+    } else {
         launch_g<16, 3>(b, ref, w, list, count, max_reads, ctr, d, scratch_bytes / 8, max_q, full, s);
         launch_g<32, 2>(b, ref, w, list, count, max_reads, ctr, d, scratch_bytes / 8, max_q, full, s, 48);
-    } else {
-        // bands of 64..127 slots (bw 32..63): 32 lanes x 4 slots
         launch_g<32, 4>(b, ref, w, list, count, max_reads, ctr, d, scratch_bytes / 8, max_q, full, s, 64);
     }
 }

@@ -566,14 +566,15 @@ void baq_wide_set_constants(const HmmConst &c) {
 
 u64 baq_wide_scratch_bytes(u32 reads, u32 max_q) {
     // whole blocks of the 32 x 2 kernel (the launch sizes its grid by the groups the scratch holds; fewer than a
-    // block launches none), and at least one block of the 16 x 3 kernel (two groups per warp)
+    // block launches none), and at least one block of the 16 x 3 and of the 32 x 4 kernel
     constexpr u64 per_block = WD_THREADS / 32;  // groups per block of the 32 x 2 kernel (one read per warp)
     const u64 rows = u64(max_q) + 2;
     const u64 per_group = rows * (2 * 64 + 1) * sizeof(float);
     u64 groups = std::min<u64>(std::max<u32>(reads, 1), 152ull * 8 * per_block);
     groups = (groups + per_block - 1) / per_block * per_block;
     const u64 block_16x3 = rows * (2 * 48 + 1) * sizeof(float) * (2 * per_block);
-    return std::max<u64>(per_group * groups, block_16x3);
+    const u64 block_32x4 = rows * (2 * 128 + 1) * sizeof(float) * per_block;
+    return std::max<u64>(per_group * groups, std::max(block_16x3, block_32x4));
 }
 
 void launch_baq_wide(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
@@ -584,6 +585,13 @@ void launch_baq_wide(const DevBatch &b, const DevRef &ref, const BatchWork &w, c
     // the scratch and the work counters, so they run one after the other.
     launch_w<16, 3>(b, ref, w, list, count, max_reads, ctr, (float *)scratch, scratch_bytes / 4, max_q, s);
     launch_w<32, 2>(b, ref, w, list, count, max_reads, ctr, (float *)scratch, scratch_bytes / 4, max_q, s, 24);
+}
+
+void launch_baq_wide64(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
+                       u32 max_reads, u32 *ctr, void *scratch, u64 scratch_bytes, u32 max_q, cudaStream_t s) {
+    if (!max_reads) return;
+    // bands of bw 32..63 (at most 127 cells) from the class-2 list: 32 lanes x 4 slots, a read per warp
+    launch_w<32, 4>(b, ref, w, list, count, max_reads, ctr, (float *)scratch, scratch_bytes / 4, max_q, s, 32);
 }
 
 void launch_baq_wide16(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,

@@ -109,6 +109,9 @@ void baq_wide_set_constants(const HmmConst &c);
 u64 baq_wide_scratch_bytes(u32 reads, u32 max_q);
 void launch_baq_wide(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
                      u32 max_reads, u32 *ctr, void *scratch, u64 scratch_bytes, u32 max_q, cudaStream_t s);
+// the same for the class-2 reads of bw 32..63: 32 lanes x 4 slots
+void launch_baq_wide64(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
+                       u32 max_reads, u32 *ctr, void *scratch, u64 scratch_bytes, u32 max_q, cudaStream_t s);
 // the same for band class 1 (bw <= 15): 16 lanes x 2 slots, two reads per warp
 void launch_baq_wide16(const DevBatch &b, const DevRef &ref, const BatchWork &w, const u32 *list, const u32 *count,
                        u32 max_reads, u32 *ctr, void *scratch, u64 scratch_bytes, u32 max_q, cudaStream_t s);
