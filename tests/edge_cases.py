@@ -176,3 +176,83 @@ def edge_case_dataset(seed=11):
     st = np.array([s for s, _ in sites], np.uint32)
     sp = np.array([e for _, e in sites], np.uint32)
     return contigs, [(st, sp)], batch, 3
+
+
+def _flank(rng, n, avoid_first=None, avoid_last=None):
+    """Random bases with no two equal neighbours, so that no homopolymer run other than the planted one sits
+    near a junction; avoid_first / avoid_last keep the ends off the run's base."""
+    out = []
+    for i in range(n):
+        while True:
+            c = DNA[rng.integers(4)]
+            if out and c == out[-1]:
+                continue
+            if i == 0 and c == avoid_first:
+                continue
+            if i == n - 1 and c == avoid_last:
+                continue
+            break
+        out.append(c)
+    return "".join(out)
+
+
+def tied_indel_dataset(seed=21, tie_quals=(2, 3, 4, 30)):
+    """Reads whose BAQ posterior at one base splits evenly between two states: a one-base deletion from a
+    two-base homopolymer run (the remaining copy aligns to either reference base with the same path weight,
+    so the two posteriors agree to about 1e-6 or closer), and a one-base insertion into a single-base run (either
+    read copy can be the inserted one; those posteriors split about 0.50 / 0.44). The reference's MAP quality
+    there is MIN_BASE_QUAL whichever state wins (device/baq.cu:673), and the capped quality
+    (device/baq.cu:895-909) is min(bq, oq) at the expected match and MIN_BASE_QUAL elsewhere, so the winner
+    only matters when the tied base's quality is below MIN_BASE_QUAL. Each placement comes with the tied-base
+    qualities tie_quals, both CIGAR placements, on both strands, at band widths 7, 14-16, 25-27 and 45-47 (a
+    second deletion of 0, 9, 20 or 40 bases later in the read).
+
+    Returns (contigs, sites, batch, num_read_groups, low_quality_tie) where low_quality_tie marks the reads
+    whose tied base has quality below MIN_BASE_QUAL."""
+    rng = np.random.default_rng(seed)
+    parts, motifs = [], []
+    pos = 0
+
+    def put(s):
+        nonlocal pos
+        parts.append(s)
+        pos += len(s)
+
+    REV = 16
+    combos = [(kind, q, flags, extra) for extra in (0, 9, 20, 40) for q in tie_quals for flags in (0, REV)
+              for kind in ("del", "ins")]
+    put(_flank(rng, 40))
+    for kind, _, _, _ in combos:
+        x = DNA[rng.integers(4)]
+        left = _flank(rng, 30, avoid_first=parts[-1][-1], avoid_last=x)
+        right = _flank(rng, 100, avoid_first=x)
+        put(left)
+        run_at = pos
+        put(x * (2 if kind == "del" else 1))
+        put(right)
+        motifs.append(run_at)
+        put(_flank(rng, 20, avoid_first=right[-1]))
+    ref = "".join(parts)
+    recs, low = [], []
+    for run_at, (kind, q, flags, extra) in zip(motifs, combos):
+        x = ref[run_at]
+        for variant in (0, 1):
+            start = run_at - 20
+            # del: variant 0 deletes the run's second copy (the read's copy is expected at the first), variant 1
+            # the first copy; ins: variant 0 inserts the read's second copy, variant 1 its first. Both variants
+            # of a placement are the same read; the second deletion follows read offset 30.
+            head = f"{21 - variant}M1{'D' if kind == 'del' else 'I'}"
+            rest = 50 - (22 if kind == "ins" else 21) + variant
+            cigar = f"{head}{rest - 19}M{extra}D19M" if extra else f"{head}{rest}M"
+            seq, quals, span = read_from_cigar(ref, start, cigar, rng)
+            if kind == "ins":
+                seq = seq[:20] + x + x + seq[22:]
+            quals = quals.copy()
+            quals[20:22 if kind == "ins" else 21] = q
+            recs.append(dict(pos=start, cigar=cigar, seq=seq, quals=quals, flags=flags, mapq=60, rg=0, span=span))
+            low.append(q < 4)
+    batch = build_batch(recs)
+    seq_syms = np.array([IUPAC[c] for c in ref], np.uint8)
+    contigs = [(pack4(seq_syms), len(ref))]
+    st = np.zeros(0, np.uint32)
+    return contigs, [(st, st.copy())], batch, 1, np.array(low, bool)

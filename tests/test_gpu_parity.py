@@ -127,6 +127,38 @@ def test_edge_cases_match_oracle(native, mode):
     assert_tables_equal(te, to)
 
 
+@pytest.mark.parametrize("mode", ["fp32", "fp64"])
+def test_tied_indel_placements_match_oracle(native, mode):
+    """One-base indels in homopolymer runs, whose tied base carries quality 2, 3, 4 or 30, in every band
+    class: stages and tables equal the oracle's."""
+    from tests.edge_cases import tied_indel_dataset
+    contigs, sites, batch, n_rg, _ = tied_indel_dataset()
+    te, se, ge = run_engine(contigs, [batch], n_rg, mode, sites)
+    to, so, go = run_oracle(contigs, [batch], n_rg, sites)
+    assert se["baq_reads"] == so["baq_reads"] == batch.num_reads
+    assert_stages_equal(batch, ge, go)
+    assert_tables_equal(te, to)
+
+
+def test_tied_states_replay_only_below_min_base_qual(native):
+    """A tied deletion placement is a state the FP32 pass cannot order. With the tied base's quality below
+    MIN_BASE_QUAL the winner changes the capped quality, so those reads replay in FP64; at quality 30 both
+    candidates cap to MIN_BASE_QUAL and the FP32 result stands."""
+    from tests.edge_cases import tied_indel_dataset
+    contigs, sites, low_batch, n_rg, _ = tied_indel_dataset(tie_quals=(2, 3))
+    t_low, s_low, _ = run_engine(contigs, [low_batch], n_rg, "fp32", sites)
+    to, _, _ = run_oracle(contigs, [low_batch], n_rg, sites)
+    assert_tables_equal(t_low, to)
+    # 32 of the 64 reads are deletion placements tied to about 1e-6 or closer
+    assert s_low["baq_fp64_escalated_reads"] >= 16, s_low
+    contigs, sites, high_batch, n_rg, _ = tied_indel_dataset(tie_quals=(30,))
+    t_high, s_high, _ = run_engine(contigs, [high_batch], n_rg, "fp32", sites)
+    to, _, _ = run_oracle(contigs, [high_batch], n_rg, sites)
+    assert_tables_equal(t_high, to)
+    # 16 tied deletion placements; without the tied-state rule every one of them would replay
+    assert s_high["baq_fp64_escalated_reads"] < 8, s_high
+
+
 def test_fp32_and_fp64_paths_agree(native):
     p, ref, batches = make_dataset("precision_20M_151bp_pe", 20000, 10000, 1_000_000)
     t32, s32, _ = run_engine(ref, batches, p.num_read_groups, "fp32")

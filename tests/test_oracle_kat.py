@@ -217,3 +217,39 @@ def test_hmm_perfect_match_is_confident():
     assert all(x >= 35 for x in oq[3:-3])
     assert [s >> 2 for s in st[3:-3]] == list(range(6, 6 + len(q) - 6))
     assert all((s & 3) == 0 for s in st)
+
+
+def _unpack4(words, start, n):
+    return np.array([(int(words[(start + i) // 8]) >> (4 * ((start + i) % 8))) & 15 for i in range(n)], np.uint8)
+
+
+def test_tied_indel_dataset_splits_the_posterior():
+    """Every one-base deletion placement of tied_indel_dataset leaves its tied base (read offset 20) with MAP
+    quality MIN_BASE_QUAL in the oracle's HMM, its MAP state a match at one of the run's two reference copies;
+    both CIGAR placements of the same read give the same HMM outputs."""
+    from tests.edge_cases import tied_indel_dataset
+    contigs, sites, b, n_rg, _ = tied_indel_dataset(tie_quals=(2, 30))
+    o = O.Oracle(n_rg)
+    O.lib().fpo_set_contig(o.h, 0, np.ascontiguousarray(contigs[0][0], np.uint32).ctypes.data, contigs[0][1])
+    o.process(b)
+    bw = o.debug_last_batch(b)["hmm"][:, 2]
+    words = contigs[0][0]
+    prev = None
+    for r in range(b.num_reads):
+        ops = b["cigars"][b["cigar_start"][r]:b["cigar_start"][r] + b["cigar_len"][r]]
+        if (int(ops[1]) >> 24) != 2:  # deletion placements only (the second CIGAR op is the one-base D)
+            continue
+        start, stop = int(b["alignment_start"][r]), int(b["alignment_stop"][r])
+        # HMM window: the aligned span plus MIN_BAND_WIDTH / 2 reference bases on each side
+        win = _unpack4(words, start - 3, stop - start + 7)
+        rl = int(b["read_len"][r])
+        query = _unpack4(b["reads"], int(b["read_start"][r]), rl)
+        qual = b["qualities"][b["qual_start"][r]:b["qual_start"][r] + rl]
+        oq, st = O.hmm(win, query, qual, int(bw[r]))
+        assert oq[20] == 4, (r, oq[18:23])
+        assert (st[20] & 3) == 0 and (st[20] >> 2) in (23, 24), (r, st[20] >> 2)
+        if prev is not None and prev[0] == start:
+            np.testing.assert_array_equal(prev[1], oq)
+            np.testing.assert_array_equal(prev[2], st)
+        prev = (start, oq, st)
+    o.close()
