@@ -18,6 +18,7 @@ class FpOptions(C.Structure):
                 ("flags", C.c_uint32), ("coalesce_reads", C.c_uint32), ("reserved", C.c_uint32)]
 FP_FLAG_REPLAY_ALL = 1
 FP_FLAG_PRECISION_TRACE = 2
+FP_FLAG_EXACT_BAQ_TAGS = 4
 
 
 class FpBatchView(C.Structure):

@@ -670,6 +670,7 @@ static fp_status submit(fp_engine *eng, const fp_batch_view *v, bool on_device) 
     const bool trace = (eng->flags & FP_FLAG_PRECISION_TRACE) && eng->baq_mode == FP_BAQ_FP32;
     w.trace32 = nullptr;
     w.trace64 = nullptr;
+    w.exact_tags = (eng->flags & FP_FLAG_EXACT_BAQ_TAGS) ? 1u : 0u;
     if (trace) {
         CK(eng->trace32.ensure(al(Q * 12 + 12)), "precision trace");
         CK(eng->trace64.ensure(al(Q * 8 + 8)), "precision trace");

@@ -628,8 +628,10 @@ __global__ void __launch_bounds__(SEG_THREADS, SEG_BLOCKS_PER_SM)
                     const int flo = capped(tlo), fhi = capped(thi);
                     if (qo <= 99) {
                         if ((flo < qo ? flo : qo) != (fhi < qo ? fhi : qo)) amb |= 1;
+                        // whether min(capped, qo) == qo, i.e. capped >= qo: monotone in t for qo <= 99
+                        if ((flo >= qo) != (fhi >= qo)) amb |= 16;
                     } else if (!(thi < 100.f && flo == fhi) && !(tlo >= 101.5f)) {
-                        amb |= 1;
+                        amb |= 1 | 16;
                     }
                     // bit 8: the state is undecided, but every candidate's MAP quality is MIN_BASE_QUAL (a rival
                     // within the bound keeps the best posterior near 1/2, so t < 5 whichever term the exact

@@ -515,8 +515,10 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
                     const int flo = capped_q(lo), fhi = capped_q(hi);
                     if (qo <= 99) {
                         if ((flo < qo ? flo : qo) != (fhi < qo ? fhi : qo)) amb |= 1;
+                        // whether min(capped, qo) == qo, i.e. capped >= qo: monotone in t for qo <= 99
+                        if ((flo >= qo) != (fhi >= qo)) amb |= 16;
                     } else if (!(hi < 100.f && flo == fhi) && !(lo >= 101.5f)) {
-                        amb |= 1;
+                        amb |= 1 | 16;
                     }
                     // bit 8: undecided state, every candidate's MAP quality MIN_BASE_QUAL (t < 5 for all)
                     if ((amb & 2) && hi < 4.9f) amb |= 8;

@@ -723,7 +723,34 @@ __global__ void __launch_bounds__(64) k_cap(DevBatch b, BatchWork w, const u32 *
                 const u8 bq = w.baq_q[qs + rb];
                 // the capped value uses the HMM quality only when the MAP state is the match at expectedPos
                 const bool at_expected = (state & 3) == 0 && (state >> 2) == expectedPos;
-                if (!exact) {
+                if (!exact && !w.exact_tags) {
+                    // Only whether the capped value equals oq reaches the tables (the covariate passes test
+                    // tag == NO_BAQ_UNCERTAINTY, as device/fractional_errors.cu:93 does): at the expected match
+                    // that is bq >= oq (undecided under bit 16), elsewhere oq == MIN_BASE_QUAL
+                    const u8 amb = w.baq_amb[qs + rb];
+                    if (amb == 7) {
+                        unbounded = true;  // a row the FP32 pass left wholly undecided
+                        escalate = true;
+                        by_state = true;
+                    } else if (amb & 6) {
+                        // undecided state: the candidates are the FP32 winner and its one rival, or (several
+                        // rivals) any state
+                        bool can_expected = true, can_other = true;
+                        if (!(amb & 4)) {
+                            const u32 alt = w.baq_alt[qs + rb];
+                            const bool alt_expected = (alt & 3) == 0 && (alt >> 2) == expectedPos;
+                            can_expected = at_expected || alt_expected;
+                            can_other = !at_expected || !alt_expected;
+                        }
+                        const bool same_at_expected = bq >= oq, same_elsewhere = oq == MIN_BASE_QUAL;
+                        if (can_expected && ((amb & 16) || (can_other && same_at_expected != same_elsewhere))) {
+                            escalate = true;
+                            by_state = true;
+                        }
+                    } else if ((amb & 16) && at_expected) {
+                        escalate = true;
+                    }
+                } else if (!exact) {
                     const u8 amb = w.baq_amb[qs + rb];
                     unbounded |= amb == 7;  // a row the FP32 pass left wholly undecided
                     if ((amb & 8) && oq >= MIN_BASE_QUAL) {

@@ -23,8 +23,10 @@ struct BatchWork {
     u8 *tag;                 // BQ tag after recode (0xFF where none)
     u8 *baq_q;               // HMM MAP quality
     u32 *baq_state;          // HMM MAP state
-    u8 *baq_amb;             // FP32 HMM: bit0 quality undecided, bit1 state undecided, bit2 more than one
-                             // other state within the bound (or no state at all)
+    u8 *baq_amb;             // FP32 HMM: 1 capped quality undecided, 2 state undecided, 4 more than one
+                             // other state within the bound (7 alone: no usable row), 8 state undecided but
+                             // every candidate's MAP quality MIN_BASE_QUAL, 16 undecided whether the capped
+                             // quality at the expected match equals the base's quality
     u16 *baq_alt;            // FP32 HMM, state undecided with one rival: the rival state
     float *frac;             // 3 x float per base (snp, ins, del fractional errors as stored in the table)
     // work lists
@@ -35,6 +37,9 @@ struct BatchWork {
                              // [22]/[23] escalations with an undecided MAP state / with undecided qualities only,
                              // [24] work counter of the class-1 replay
     u32 *esc_list;
+    // FP32 mode: 1 certifies every capped quality exactly (FP_FLAG_EXACT_BAQ_TAGS), 0 only whether it equals
+    // the base's quality (the one property of a BQ tag the covariate tables depend on)
+    u32 exact_tags;
     // precision trace (FP_FLAG_PRECISION_TRACE; null otherwise): per base the FP32 kernels' pre-floor MAP
     // quality t and its certified interval [lo, hi] (t = NaN where the FP32 pass has no value), and the
     // plain FP64 path's t

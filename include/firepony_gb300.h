@@ -79,6 +79,12 @@ typedef struct {
  * compare the two pre-floor MAP qualities per base; see fp_engine_get_precision_stats. Costs one plain
  * FP64 BAQ pass per batch. No reference counterpart (the reference has only the FP64 HMM). */
 #define FP_FLAG_PRECISION_TRACE 2u
+/* Check: in FP32 mode, certify every base's capped BAQ quality exactly (BQ tags identical to the FP64
+ * path's), not only whether it equals the base's quality. The reference consumes the BQ tags only through
+ * that test (fractional_errors.cu:93, tag == NO_BAQ_UNCERTAINTY), so the tables are the same either way;
+ * this flag makes the engine's BQ tags (fp_engine_debug_last_batch) match the FP64 path's as well, at the
+ * cost of more FP64 replays. */
+#define FP_FLAG_EXACT_BAQ_TAGS 4u
 
 /* One alignment batch, mirroring alignment_batch_storage<host> (alignment_data.h:125-173). The engine
  * borrows these host buffers only for the duration of fp_engine_submit_batch. */
