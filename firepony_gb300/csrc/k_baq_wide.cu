@@ -36,8 +36,11 @@ namespace {
 
 constexpr u32 FULL = 0xffffffffu;
 constexpr int WD_THREADS = 128;
-constexpr float FWD_SCALE = 18446744073709551616.0f;          // 2^64 (forward rows sum to 2^64)
-constexpr float BWD_INIT = 79228162514264337593543950336.0f;  // 2^96 = 2^64 (sLast) x 2^32 (backward factor)
+// Forward rows sum to 2^120 and backward values carry 2^-24 (their posterior products 2^96): a row's
+// unscaled sum stays below 1.25 * 2^120, and a forward cell is flushed only below 2^-198 of its row, so the
+// forward flush bound (which grows by 1/s(i) per row) stays small even for reads whose rows drop sharply
+constexpr float FWD_SCALE = 1329227995784915872903807060280344576.0f;  // 2^120
+constexpr float BWD_INIT = 79228162514264337593543950336.0f;             // 2^96 = 2^120 (sLast) x 2^-24
 
 constexpr float FLUSH = 3.3087224502121107e-24f;  // 2^-78
 
@@ -311,11 +314,13 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
             // posterior sum through backward values <= 1 (reference units), i.e. at most e * prod(inv of the
             // rows after j) / sLast of the total; 1.01 covers the rounding of the bound itself
             const float kf_all = gsum<G>(kf);
-            ef = kf_all > 0.0f ? 1.01f * FLUSH * kf_all / sLast : 0.0f;
+            // (a bound below the normal range is kept at 2^-125, above any value that rounds there)
+            ef = kf_all > 0.0f ? fmaxf(1.01f * FLUSH * kf_all / sLast, 2.350988701644575e-38f) : 0.0f;
             if (!(ef < 1.0f)) ef = __int_as_float(0x7f800000);
             const float sQ = qL >= 1 ? FROW(qL)[2 * WC] : 1.0f;
-            // sM / s(qL) / sLast in reference units, times 2^32: sQ carries 2^64 unless qL == 1, sLast 2^64
-            const float v = ((sM / sQ) * (qL >= 2 ? FWD_SCALE : 1.0f) / sLast) * BWD_INIT;
+            // sM / s(qL) / sLast in reference units, times 2^-24: sQ carries 2^120 unless qL == 1, sLast 2^120
+            // (grouped so that no intermediate leaves the normal range)
+            const float v = ((sM * (qL >= 2 ? FWD_SCALE : 1.0f)) / sQ) * (BWD_INIT / sLast);
 #pragma unroll
             for (int j = 0; j < NS; j++) {
                 const int s = l + j * G;
@@ -335,7 +340,7 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
         const float dt = 4.343f * rel / (1.0f - rel) + 1e-4f;
         // backward flushes, relative to the posterior total, over the rows done so far (qL down to i): an error
         // e in a backward value of row i' reaches every posterior sum through that cell's forward value, at
-        // most the forward row sum 2^64, i.e. at most e * 2^64 / (row i' posterior sum) of the total
+        // most the forward row sum 2^120, i.e. at most e * 2^120 / (row i' posterior sum) of the total
         float eb = 0.0f;
 
         // ---- backward fused with MAP, rows qL..1 of every group (t steps back from its own last row) ----
@@ -380,7 +385,7 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
                     }
                 }
                 __syncwarp();
-                // 1 / s(i) in reference units: s(i) carries 2^64 for rows after the first
+                // 1 / s(i) in reference units: s(i) carries 2^120 for rows after the first
                 const float yy = act ? (i == 1 ? 1.0f : FWD_SCALE) / FROW(i)[2 * WC] : 0.0f;
                 float cbpost = 0.0f;
 #pragma unroll
