@@ -3,13 +3,16 @@
 // NS slots, WC = G*NS >= 2*bw+1; 32/G reads per warp). A thread-per-read kernel cannot hold a band this wide in
 // registers, and the exact FP64 kernel costs ~64 cycles per FP64 warp instruction on this GPU.
 //
-// Every cell takes the operations of k_baq_tpr<float> (the same products and sums in the same grouping), so
-// the error analysis of that file applies unchanged: forward and backward values carry
-// eps <= (7 qL + 2 refLen + 8) 2^-24, a posterior term eps_z = 2 eps + 2^-24, a sum of at most 2 WC terms adds
-// 2 WC 2^-24 (in any order: the row and posterior sums here are lane partial sums combined by shuffles), and
-// the decisions (MAP quality within dt of a rounding boundary, runner-up state within the bound) are the same.
-// The forward row sums only set the row scaling, a common factor that cancels in every posterior ratio, and
-// the chains along a row (the D recurrences) run on the group's first lane in slot order.
+// Every M and I cell takes the operations of k_baq_tpr<float> (the same products and sums in the same
+// grouping). The D recurrence along a row, D(k) = c(k) + m8 * D(k-1), is a linear scan: D(k) =
+// sum_n m8^n c(k-n), computed per segment of G slots in log2(G) shuffle steps over the group's lanes plus a
+// carry from the segment below, instead of a serial chain on one lane. A path's D run within a row then takes
+// a fixed number of roundings (2 to enter, 2 per scan level, 2 per carry) instead of 2 per D step, so forward
+// and backward values carry eps <= (7 qL + D_RUN min(qL, refLen) + 8) 2^-24 (at most one D run per row), a
+// posterior term eps_z = 2 eps + 2^-24, a sum of at most 2 WC terms adds 2 WC 2^-24 (in any order: the row
+// and posterior sums here are lane partial sums combined by shuffles), and the decisions (MAP quality within
+// dt of a rounding boundary, runner-up state within the bound) are taken as in k_baq_tpr<float>. The forward
+// row sums only set the row scaling, a common factor that cancels in every posterior ratio.
 //
 // Cells far from the alignment decay by many orders of magnitude across a wide band. Instead of giving up on
 // a read with such a cell, a computed cell value below FLUSH is replaced by zero. Every operand of the
@@ -19,7 +22,9 @@
 // absolute error below FLUSH, whose effect on the posterior terms is bounded separately (backward values are
 // at most 1 and forward values at most the row sum in the scaled units; see the error terms below) and added
 // to the decision margins as an absolute error. Posterior products of kept values may still underflow: each
-// adds at most 2^-150.
+// adds at most 2^-150. In the D scans a partial sum times a high power of m8 may fall below the normal range;
+// it enters a fused add, and a kept D value (at least FLUSH) then carries at most 2^-150 per scan step from
+// it, below 2^-70 of the value, inside the 8 spare roundings of eps.
 //
 // Slot s of row i holds cell k = s + x(i), x(i) = max(i - bw, 0); rows are exchanged through per-group shared
 // buffers indexed by slot + 1 with zero sentinels. A group whose read has a band wider than WC takes no read
@@ -92,6 +97,8 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
     constexpr int WPB = WD_THREADS / 32;
     constexpr int ROWF = 2 * WC + 1;    // scratch floats per row
     constexpr int XB = 2 * WC + 2;      // exchange buffer length
+    constexpr int LOG2G = G == 32 ? 5 : (G == 16 ? 4 : (G == 8 ? 3 : (G == 4 ? 2 : 1)));
+    static_assert((1 << LOG2G) == G, "G is a power of two");
     __shared__ float s_em[256], s_mis[256];
     // per group: forward previous row (M, I, D), backward next row (M, I), three exchange buffers
     __shared__ float s_buf[WPB][GPW][8][XB];
@@ -106,6 +113,22 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
 
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int g = lane / G, l = lane % G;
+    // powers of m8 = 0.1 for the D scans, each rounded once to float from a double product (relative error
+    // of the double below 2^-48): m8^(2^lv) per scan level, m8^(l+1) and m8^(G-l) for the segment carries
+    float m8p[LOG2G], m8up, m8dn;
+    {
+        double p = 1.0, pu = 0.0, pd = 0.0;
+#pragma unroll
+        for (int n = 1; n <= G; n++) {
+            p *= 0.1;
+            for (int lv = 0; lv < LOG2G; lv++)
+                if (n == (1 << lv)) m8p[lv] = float(p);
+            if (n == l + 1) pu = p;
+            if (n == G - l) pd = p;
+        }
+        m8up = float(pu);
+        m8dn = float(pd);
+    }
     float *PM = s_buf[wib][g][0], *PI = s_buf[wib][g][1], *PD = s_buf[wib][g][2];
     float *QM = s_buf[wib][g][3], *QI = s_buf[wib][g][4];
     float *X0 = s_buf[wib][g][5], *X1 = s_buf[wib][g][6];
@@ -164,6 +187,7 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
         const float m0 = float((1 - GOP - GOP) * (1 - dsM)), m1 = float(GOP * (1 - dsM)), m2 = m1;
         const float m3 = float((1 - 0.1) * (1 - dsM)), m4 = float(0.1 * (1 - dsM));
         const float m6 = float(1 - 0.1), m8 = float(0.1);
+        (void)m8;
         const float EIm1 = EI * m1, EIm4 = EI * m4;
         // forward flush errors in units of FLUSH, carried to row qL's scale: K = (K + before-scaling flushes)
         // * inv + after-scaling flushes, row by row (each lane its own flushes; the terms add up)
@@ -221,9 +245,6 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
             const bool slide = i > bw;
             const u8 qy = act ? QRY(i - 1) : 0, qq = act ? QUL(i - 1) : 0;
             qmax = qmax > qq ? qmax : qq;
-            // the D chain visits only the slots holding band cells of some group (zeros elsewhere)
-            const int slo = int(__reduce_min_sync(FULL, u32(act ? (beg - x > 0 ? beg - x : 0) : WC)));
-            const int shi = int(__reduce_max_sync(FULL, u32(act ? (end - x < WC - 1 ? end - x : WC - 1) : 0)));
             // M and I of every slot from the previous row; m2 * M feeds the D chain of the next slot
             float mI[NS];
             float cpre = 0.0f;  // this lane's flushes of the row before its scaling
@@ -248,15 +269,25 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
                 X0[s + 1] = m2 * m;
             }
             __syncwarp();
-            // D(k) = m2 * M(k-1) + m8 * D(k-1) along the row on the group's first lane (zero below the band;
-            // past it the chain runs on but those slots are discarded)
-            if (l == 0) {
-                float d = 0.0f;  // (zero at and below the lowest band slot)
-                for (int s = slo; s <= shi; s++) {
-                    d = (s == 0 ? 0.0f : X0[s]) + m8 * d;
-                    // (a chain value past the band is discarded; its flush only adds to the bound)
-                    flush(d, cpre);
+            // D(k) = m2 * M(k-1) + m8 * D(k-1) along the row, as D(k) = sum_n m8^n * m2 * M(k-1-n): per segment
+            // of G slots a scan over the group's lanes, then the carry m8^(l+1) * D(top slot of the segment
+            // below). Zero below the band; values past it are discarded (only in-band flushes count)
+            {
+                float carry = 0.0f;
+#pragma unroll
+                for (int j = 0; j < NS; j++) {
+                    const int s = l + j * G, k = s + x;
+                    float d = s == 0 ? 0.0f : X0[s];
+#pragma unroll
+                    for (int lv = 0; lv < LOG2G; lv++) {
+                        const float up = __shfl_up_sync(FULL, d, 1 << lv, G);
+                        if (l >= (1 << lv)) d = fmaf(m8p[lv], up, d);
+                    }
+                    if (j > 0) d = fmaf(m8up, carry, d);
+                    if (act && k >= beg && k <= end) flush(d, cpre);
+                    else if (d < FLUSH) d = 0.0f;
                     X1[s] = d;
+                    carry = __shfl_sync(FULL, d, G - 1, G);
                 }
             }
             __syncwarp();
@@ -333,7 +364,11 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
         }
         // certified FP32 bounds of k_baq_tpr (2 WC terms at most per posterior sum)
         const float u = 5.9604644775390625e-8f;
-        const float eps = float((7.0 * qL + 2.0 * refLen + 8.0) * 5.9604644775390625e-8);
+        // a path's D run within a row (at most one per row, so at most min(qL, refLen) runs) takes 2 roundings
+        // to enter (m2 and its product), 2 per scan level (an m8 power and the fused add) and 2 per segment
+        // carry, whatever its length
+        constexpr int D_RUN = 2 + 2 * LOG2G + 2 * (NS - 1);
+        const float eps = float((7.0 * qL + double(D_RUN) * (qL < refLen ? qL : refLen) + 8.0) * 5.9604644775390625e-8);
         const float eps_z = 2.0f * eps + u;
         const float rel = 2.0f * (eps_z + 2.0f * WC * u) + u;
         const float rel_state = 2.0f * eps_z + 2.0f * u;
@@ -352,8 +387,6 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
             const int end = refLen < i + bw ? refLen : i + bw;
             const int x = i - bw > 0 ? i - bw : 0;
             if (t > 0) {
-                const int slo = int(__reduce_min_sync(FULL, u32(act ? (beg - x > 0 ? beg - x : 0) : WC)));
-                const int shi = int(__reduce_max_sync(FULL, u32(act ? (end - x < WC - 1 ? end - x : WC - 1) : 0)));
                 const bool grow = i < bw;  // row i+1 still in the growing band
                 const bool y = i > 1;
                 const u8 qy1 = act ? QRY(i) : 0, qq1 = act ? QUL(i) : 0;
@@ -373,16 +406,27 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
                     X0[s] = inb ? e * m6 : 0.0f;
                 }
                 __syncwarp();
-                // B_D(k) = (e * m6 + m8 * B_D(k+1)) * y, descending along the row on the group's first lane
-                if (l == 0) {
-                    float d = 0.0f;  // (zero above the highest band slot)
-                    X1[WC] = 0.0f;
-                    X1[shi + 1] = 0.0f;
-                    for (int s = shi; s >= slo; s--) {
-                        d = y ? X0[s] + m8 * d : 0.0f;
-                        flush(d, cbpre);
+                // B_D(k) = (e * m6 + m8 * B_D(k+1)) * y, descending along the row: per segment a scan over the
+                // group's lanes, then the carry m8^(G-l) * B_D(bottom slot of the segment above)
+                {
+                    float carry = 0.0f;
+#pragma unroll
+                    for (int j = NS - 1; j >= 0; j--) {
+                        const int s = l + j * G, k = s + x;
+                        float d = X0[s];
+#pragma unroll
+                        for (int lv = 0; lv < LOG2G; lv++) {
+                            const float dn = __shfl_down_sync(FULL, d, 1 << lv, G);
+                            if (l + (1 << lv) < G) d = fmaf(m8p[lv], dn, d);
+                        }
+                        if (j < NS - 1) d = fmaf(m8dn, carry, d);
+                        if (!y) d = 0.0f;
+                        if (act && k >= beg && k <= end) flush(d, cbpre);
+                        else if (d < FLUSH) d = 0.0f;
                         X1[s] = d;
+                        carry = __shfl_sync(FULL, d, 0, G);
                     }
+                    if (l == 0) X1[WC] = 0.0f;  // (above the top slot)
                 }
                 __syncwarp();
                 // 1 / s(i) in reference units: s(i) carries 2^120 for rows after the first
