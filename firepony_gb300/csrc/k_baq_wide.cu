@@ -41,11 +41,11 @@ namespace {
 
 constexpr u32 FULL = 0xffffffffu;
 constexpr int WD_THREADS = 128;
-// Forward rows sum to 2^120 and backward values carry 2^-24 (their posterior products 2^96): a row's
-// unscaled sum stays below 1.25 * 2^120, and a forward cell is flushed only below 2^-198 of its row, so the
+// Forward rows sum to 2^110 and backward values carry 2^-14 (their posterior products 2^96): a row's
+// unscaled sum stays below 1.25 * 2^110, and a forward cell is flushed only below 2^-188 of its row, so the
 // forward flush bound (which grows by 1/s(i) per row) stays small even for reads whose rows drop sharply
-constexpr float FWD_SCALE = 1329227995784915872903807060280344576.0f;  // 2^120
-constexpr float BWD_INIT = 79228162514264337593543950336.0f;             // 2^96 = 2^120 (sLast) x 2^-24
+constexpr float FWD_SCALE = 1298074214633706907132624082305024.0f;  // 2^110
+constexpr float BWD_INIT = 79228162514264337593543950336.0f;         // 2^96 = 2^110 (sLast) x 2^-14
 
 constexpr float FLUSH = 3.3087224502121107e-24f;  // 2^-78
 
@@ -349,7 +349,7 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
             ef = kf_all > 0.0f ? fmaxf(1.01f * FLUSH * kf_all / sLast, 2.350988701644575e-38f) : 0.0f;
             if (!(ef < 1.0f)) ef = __int_as_float(0x7f800000);
             const float sQ = qL >= 1 ? FROW(qL)[2 * WC] : 1.0f;
-            // sM / s(qL) / sLast in reference units, times 2^-24: sQ carries 2^120 unless qL == 1, sLast 2^120
+            // sM / s(qL) / sLast in reference units, times 2^-14: sQ carries 2^110 unless qL == 1, sLast 2^110
             // (grouped so that no intermediate leaves the normal range)
             const float v = ((sM * (qL >= 2 ? FWD_SCALE : 1.0f)) / sQ) * (BWD_INIT / sLast);
 #pragma unroll
@@ -375,7 +375,7 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
         const float dt = 4.343f * rel / (1.0f - rel) + 1e-4f;
         // backward flushes, relative to the posterior total, over the rows done so far (qL down to i): an error
         // e in a backward value of row i' reaches every posterior sum through that cell's forward value, at
-        // most the forward row sum 2^120, i.e. at most e * 2^120 / (row i' posterior sum) of the total
+        // most the forward row sum 2^110, i.e. at most e * 2^110 / (row i' posterior sum) of the total
         float eb = 0.0f;
 
         // ---- backward fused with MAP, rows qL..1 of every group (t steps back from its own last row) ----
@@ -429,7 +429,7 @@ __global__ void __launch_bounds__(WD_THREADS) k_baq_wide(DevBatch b, DevRef dref
                     if (l == 0) X1[WC] = 0.0f;  // (above the top slot)
                 }
                 __syncwarp();
-                // 1 / s(i) in reference units: s(i) carries 2^120 for rows after the first
+                // 1 / s(i) in reference units: s(i) carries 2^110 for rows after the first
                 const float yy = act ? (i == 1 ? 1.0f : FWD_SCALE) / FROW(i)[2 * WC] : 0.0f;
                 float cbpost = 0.0f;
 #pragma unroll
