@@ -271,6 +271,10 @@ def run_batched(args):
         out["baq_fp64_escalated_reads"] = st["baq_fp64_escalated_reads"]
         out["baq_escalated_by_cause"] = st["baq_escalated_by_cause"]
         out["baq_escalated_undecided_rows"] = st["baq_escalated_undecided_rows"]
+        # device time from each BAQ stage's start to the end of the class-0 FP32 path, the class-0 replay (which
+        # follows the class-2 FP32 kernels on the same stream), the class-1 FP32 path and the class-1 replay,
+        # summed over the device batches
+        out["baq_path_ms"] = [round(v, 2) for v in st["baq_path_ms"]]
         # bounded sample: per batch / coalesced / plain FP64 coalesced, identical tables
         sample = pinned[:args.batched_sample]
         sreads = int(sum(b.num_reads for b in sample))
