@@ -72,3 +72,33 @@ def test_tied_map_states_cap_at_min_base_qual():
     at_expected = np.minimum(min_base_qual, oq)
     elsewhere = np.full_like(oq, min_base_qual)
     assert ((at_expected == elsewhere) == (oq >= min_base_qual)).all()
+
+
+def test_tag_property_is_monotone_in_t():
+    """The FP32 kernels decide, per base, whether the capped quality equals the base's quality (the BQ tag is
+    NO_BAQ_UNCERTAINTY), the one property of the tag the reference reads (fractional_errors.cu:93). At the
+    expected match the capped value is min(capped_q(t), oq) with capped_q the reference's MAP quality
+    (device/baq.cu:673: floor, clamped to [MIN_BASE_QUAL, 99], 100 kept); the test capped_q(t) >= oq is
+    monotone in t for oq <= 99, so the endpoints of a certified interval decide it (baq_amb bit 16). Elsewhere
+    the capped value is MIN_BASE_QUAL, equal to oq exactly when oq == 4."""
+    min_base_qual = 4
+
+    def capped_q(t):
+        t = np.asarray(t, np.float64)
+        k = np.where(np.isnan(t), 0, np.where(t >= 2147483520.0, 2147483647, np.floor(np.nan_to_num(t, neginf=-1e18))))
+        k = np.maximum(k, -2.0 ** 31)
+        return np.where(k > 100, 99, np.where(k < min_base_qual, min_base_qual, k)).astype(np.int64)
+
+    t = np.concatenate([[-np.inf], np.linspace(-5.0, 130.0, 270_001), [np.inf]])
+    for oq in range(0, 100):
+        same = np.minimum(capped_q(t), oq) == oq
+        # monotone: once true, true for every larger t
+        first = np.argmax(same) if same.any() else len(t)
+        assert same[first:].all(), oq
+        if oq <= min_base_qual:
+            assert same.all()
+    # qualities above 100 never equal a capped value (the kernels leave such reads to the exact replay)
+    assert not (capped_q(t) >= 101).any()
+    # elsewhere than the expected match
+    oq = np.arange(0, 94)
+    assert ((np.full_like(oq, min_base_qual) == oq) == (oq == min_base_qual)).all()
