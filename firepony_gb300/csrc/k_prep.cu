@@ -656,6 +656,8 @@ __global__ void __launch_bounds__(PREP_WARPS * 32) k_prep(DevBatch b, DevRef ref
 // escalation list and the exact replay's capping rewrites its values. A state left undecided by a rival
 // within the bound (baq_amb bit 2) caps at MIN_BASE_QUAL whichever candidate wins whenever the kernel also
 // proved every candidate's MAP quality to be MIN_BASE_QUAL (bit 8) and the original quality is at least that.
+constexpr int CAP_PF = 4;  // chunks of 32 events whose loads k_cap issues together
+
 __global__ void __launch_bounds__(64) k_cap(DevBatch b, BatchWork w, const u32 *list, const u32 *count, int exact) {
     constexpr u32 FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -700,84 +702,111 @@ __global__ void __launch_bounds__(64) k_cap(DevBatch b, BatchWork w, const u32 *
         u32 end = n;
         u32 refI_c = 0, numD_c = 0, readI_c = 0;
         bool escalate = false, by_state = false, unbounded = false;
-        for (u32 c = baq_start; c < end; c += 32) {
-            const u32 i = c + lane;
-            const u32 rcv = i < end ? rc[i] : u32(U16_NONE);
-            const u16 rb = u16(rcv & 0xFFFF);
-            const u32 past = __ballot_sync(FULL, rb != U16_NONE && rb > wcl.y);
-            if (past) end = c + __ffs(past) - 1;
-            const bool in = i < end;
-            const u8 t = in ? ty[i] : EV_S;
-            const bool isM = in && t == EV_M, isI = in && t == EV_I, isD = in && t == EV_D;
-            const bool isRef = in && (t == EV_S || t == EV_D || t == EV_M);
-            const u32 mRef = __ballot_sync(FULL, isRef), mD = __ballot_sync(FULL, isD);
-            const u32 mRead = __ballot_sync(FULL, isM || isI);
-            if (isI) {
-                w.tag[qs + rb] = NO_BAQ_UNCERTAINTY;
-            } else if (isM) {
-                const u32 refI = refI_c + __popc(mRef & lt), numD = numD_c + __popc(mD & lt);
-                const u32 readI = readI_c + __popc(mRead & lt);
-                const u32 expectedPos = refI - u32(int(refOffset)) + (i - numD - baq_start - readI) + u32(int(read_shift));
-                const u32 state = w.baq_state[qs + rb];
-                const u8 oq = b.quals[qs + rb];
-                const u8 bq = w.baq_q[qs + rb];
-                // the capped value uses the HMM quality only when the MAP state is the match at expectedPos
-                const bool at_expected = (state & 3) == 0 && (state >> 2) == expectedPos;
-                if (!exact && !w.exact_tags) {
-                    // Only whether the capped value equals oq reaches the tables (the covariate passes test
-                    // tag == NO_BAQ_UNCERTAINTY, as device/fractional_errors.cu:93 does): at the expected match
-                    // that is bq >= oq (undecided under bit 16), elsewhere oq == MIN_BASE_QUAL
-                    const u8 amb = w.baq_amb[qs + rb];
-                    if (amb == 7) {
-                        unbounded = true;  // a row the FP32 pass left wholly undecided
-                        escalate = true;
-                        by_state = true;
-                    } else if (amb & 6) {
-                        // undecided state: the candidates are the FP32 winner and its one rival, or (several
-                        // rivals) any state
-                        bool can_expected = true, can_other = true;
-                        if (!(amb & 4)) {
+        // CAP_PF chunks of 32 events at a time: their events and the HMM outputs of their M bases are loaded
+        // together (one round of dependent loads per CAP_PF chunks), then the chunks are walked in order. The
+        // walk ends inside a group only (the chunk holding `end`), so every group starts with end == n; loads
+        // past `end` stay inside the read (its bases and events) and are not used.
+        for (u32 c0 = baq_start; c0 < end; c0 += 32 * CAP_PF) {
+            u32 rc_v[CAP_PF], st_v[CAP_PF];
+            u8 ty_v[CAP_PF], oq_v[CAP_PF], bq_v[CAP_PF], amb_v[CAP_PF];
+#pragma unroll
+            for (int q = 0; q < CAP_PF; q++) {
+                const u32 i = c0 + 32 * q + lane;
+                rc_v[q] = i < end ? rc[i] : u32(U16_NONE);
+                ty_v[q] = i < end ? ty[i] : u8(EV_S);
+            }
+#pragma unroll
+            for (int q = 0; q < CAP_PF; q++) {
+                const u16 rb = u16(rc_v[q] & 0xFFFF);
+                const bool m = ty_v[q] == EV_M && rb != U16_NONE;
+                st_v[q] = m ? w.baq_state[qs + rb] : 0u;
+                oq_v[q] = m ? b.quals[qs + rb] : u8(0);
+                bq_v[q] = m ? w.baq_q[qs + rb] : u8(0);
+                amb_v[q] = m && !exact ? w.baq_amb[qs + rb] : u8(0);
+            }
+#pragma unroll
+            for (int q = 0; q < CAP_PF; q++) {
+                const u32 c = c0 + 32 * q;
+                if (c >= end) break;  // (end is the same in every lane)
+                const u32 i = c + lane;
+                const u32 rcv = i < end ? rc_v[q] : u32(U16_NONE);
+                const u16 rb = u16(rcv & 0xFFFF);
+                const u32 past = __ballot_sync(FULL, rb != U16_NONE && rb > wcl.y);
+                if (past) end = c + __ffs(past) - 1;
+                const bool in = i < end;
+                const u8 t = in ? ty_v[q] : u8(EV_S);
+                const bool isM = in && t == EV_M, isI = in && t == EV_I, isD = in && t == EV_D;
+                const bool isRef = in && (t == EV_S || t == EV_D || t == EV_M);
+                const u32 mRef = __ballot_sync(FULL, isRef), mD = __ballot_sync(FULL, isD);
+                const u32 mRead = __ballot_sync(FULL, isM || isI);
+                if (isI) {
+                    w.tag[qs + rb] = NO_BAQ_UNCERTAINTY;
+                } else if (isM) {
+                    const u32 refI = refI_c + __popc(mRef & lt), numD = numD_c + __popc(mD & lt);
+                    const u32 readI = readI_c + __popc(mRead & lt);
+                    const u32 expectedPos =
+                        refI - u32(int(refOffset)) + (i - numD - baq_start - readI) + u32(int(read_shift));
+                    const u32 state = st_v[q];
+                    const u8 oq = oq_v[q];
+                    const u8 bq = bq_v[q];
+                    // the capped value uses the HMM quality only when the MAP state is the match at expectedPos
+                    const bool at_expected = (state & 3) == 0 && (state >> 2) == expectedPos;
+                    if (!exact && !w.exact_tags) {
+                        // Only whether the capped value equals oq reaches the tables (the covariate passes test
+                        // tag == NO_BAQ_UNCERTAINTY, as device/fractional_errors.cu:93 does): at the expected match
+                        // that is bq >= oq (undecided under bit 16), elsewhere oq == MIN_BASE_QUAL
+                        const u8 amb = amb_v[q];
+                        if (amb == 7) {
+                            unbounded = true;  // a row the FP32 pass left wholly undecided
+                            escalate = true;
+                            by_state = true;
+                        } else if (amb & 6) {
+                            // undecided state: the candidates are the FP32 winner and its one rival, or (several
+                            // rivals) any state
+                            bool can_expected = true, can_other = true;
+                            if (!(amb & 4)) {
+                                const u32 alt = w.baq_alt[qs + rb];
+                                const bool alt_expected = (alt & 3) == 0 && (alt >> 2) == expectedPos;
+                                can_expected = at_expected || alt_expected;
+                                can_other = !at_expected || !alt_expected;
+                            }
+                            const bool same_at_expected = bq >= oq, same_elsewhere = oq == MIN_BASE_QUAL;
+                            if (can_expected && ((amb & 16) || (can_other && same_at_expected != same_elsewhere))) {
+                                escalate = true;
+                                by_state = true;
+                            }
+                        } else if ((amb & 16) && at_expected) {
+                            escalate = true;
+                        }
+                    } else if (!exact) {
+                        const u8 amb = amb_v[q];
+                        unbounded |= amb == 7;  // a row the FP32 pass left wholly undecided
+                        if ((amb & 8) && oq >= MIN_BASE_QUAL) {
+                            // undecided state whose candidates all have MAP quality MIN_BASE_QUAL: min(bq, oq) at
+                            // the expected match and MIN_BASE_QUAL elsewhere are the same value
+                        } else if (amb & 4) {
+                            escalate = true;
+                            by_state = true;
+                        } else if (amb & 2) {
+                            // one rival state: decided when neither state is the match at expectedPos (the value is
+                            // MIN_BASE_QUAL whichever wins)
                             const u32 alt = w.baq_alt[qs + rb];
                             const bool alt_expected = (alt & 3) == 0 && (alt >> 2) == expectedPos;
-                            can_expected = at_expected || alt_expected;
-                            can_other = !at_expected || !alt_expected;
-                        }
-                        const bool same_at_expected = bq >= oq, same_elsewhere = oq == MIN_BASE_QUAL;
-                        if (can_expected && ((amb & 16) || (can_other && same_at_expected != same_elsewhere))) {
+                            if (at_expected || alt_expected) {
+                                escalate = true;
+                                by_state = true;
+                            }
+                        } else if ((amb & 1) && at_expected) {
                             escalate = true;
-                            by_state = true;
                         }
-                    } else if ((amb & 16) && at_expected) {
-                        escalate = true;
                     }
-                } else if (!exact) {
-                    const u8 amb = w.baq_amb[qs + rb];
-                    unbounded |= amb == 7;  // a row the FP32 pass left wholly undecided
-                    if ((amb & 8) && oq >= MIN_BASE_QUAL) {
-                        // undecided state whose candidates all have MAP quality MIN_BASE_QUAL: min(bq, oq) at
-                        // the expected match and MIN_BASE_QUAL elsewhere are the same value
-                    } else if (amb & 4) {
-                        escalate = true;
-                        by_state = true;
-                    } else if (amb & 2) {
-                        // one rival state: decided when neither state is the match at expectedPos (the value is
-                        // MIN_BASE_QUAL whichever wins)
-                        const u32 alt = w.baq_alt[qs + rb];
-                        const bool alt_expected = (alt & 3) == 0 && (alt >> 2) == expectedPos;
-                        if (at_expected || alt_expected) {
-                            escalate = true;
-                            by_state = true;
-                        }
-                    } else if ((amb & 1) && at_expected) {
-                        escalate = true;
-                    }
+                    const u8 v = at_expected ? (bq < oq ? bq : oq) : u8(MIN_BASE_QUAL);
+                    w.tag[qs + rb] = u8(u8(oq + 64) - v);
                 }
-                const u8 v = at_expected ? (bq < oq ? bq : oq) : u8(MIN_BASE_QUAL);
-                w.tag[qs + rb] = u8(u8(oq + 64) - v);
+                refI_c += __popc(mRef);
+                numD_c += __popc(mD);
+                readI_c += __popc(mRead);
             }
-            refI_c += __popc(mRef);
-            numD_c += __popc(mD);
-            readI_c += __popc(mRead);
         }
         const bool need_update = readI_c == u32(wcl.y - wcl.x + 1);
         if (!need_update) {
