@@ -518,8 +518,15 @@ constexpr int PREP_WARPS = 8;
 // written out once.
 __global__ void __launch_bounds__(PREP_WARPS * 32) k_prep(DevBatch b, DevRef ref, BatchWork w) {
     __shared__ u8 s_bf[PREP_WARPS][512];
+    // per warp, over its reads: band cells per class, BAQ reads, longest query, widest band per class; added to
+    // the batch counters once, when the warp has no reads left
+    __shared__ unsigned long long s_cells[PREP_WARPS][3];
+    __shared__ u32 s_agg[PREP_WARPS][5];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     u8 *sbf = s_bf[wib];
+    if (lane < 3) s_cells[wib][lane] = 0;
+    if (lane < 5) s_agg[wib][lane] = 0;
+    __syncwarp();
     for (u32 r = blockIdx.x * PREP_WARPS + wib; r < b.R; r += gridDim.x * PREP_WARPS) {
         const u32 qs = b.qual_start[r];
         const u32 rlen = b.read_len[r];
@@ -635,13 +642,19 @@ __global__ void __launch_bounds__(PREP_WARPS * 32) k_prep(DevBatch b, DevRef ref
             const i64 m = qL < B ? qL : B;
             const i64 sum_lo = tri(qL) - qL * B + (m * (B + 1) - tri(m));
             const u64 cells = u64(sum_hi - sum_lo + qL);
-            atomicAdd(reinterpret_cast<unsigned long long *>(w.counters + 16) + cls, (unsigned long long)cells);
-            atomicAdd(&w.counters[6], 1u);
-            atomicMax(&w.counters[7], u32(wcl.y - wcl.x + 1));
-            atomicMax(&w.counters[12 + cls], u32(bw));
+            s_cells[wib][cls] += cells;
+            s_agg[wib][0] += 1u;
+            s_agg[wib][1] = max(s_agg[wib][1], u32(wcl.y - wcl.x + 1));
+            s_agg[wib][2 + cls] = max(s_agg[wib][2 + cls], u32(bw));
         }
         __syncwarp();
     }
+    __syncwarp();
+    if (lane < 3 && s_cells[wib][lane])
+        atomicAdd(reinterpret_cast<unsigned long long *>(w.counters + 16) + lane, s_cells[wib][lane]);
+    if (lane == 3 && s_agg[wib][0]) atomicAdd(&w.counters[6], s_agg[wib][0]);
+    if (lane == 4 && s_agg[wib][1]) atomicMax(&w.counters[7], s_agg[wib][1]);
+    if (lane >= 5 && lane < 8 && s_agg[wib][2 + lane - 5]) atomicMax(&w.counters[12 + lane - 5], s_agg[wib][2 + lane - 5]);
 }
 
 // ---------------------------------------------------------------------------------------------------
